@@ -1,0 +1,605 @@
+// Device side of the GB300 Brandes engine.
+//
+// One "unit" is one source vertex in one CSR segment (a whole graph, the induced
+// subgraph of one Louvain cluster, or one graph of a multi-graph batch).  A unit runs
+// the three passes of the reference's single-source Brandes
+// (ExactBrandesBC.h:97-161 forward, ExactBrandesBC.h:73-90 backward):
+//
+//   1. distances   near-far delta-stepping over int32 weights: near queue = vertices with
+//                  tentative distance below the bucket threshold T, far pile = the rest;
+//                  relaxation by atomicMin on int32 distances, warp-cooperative over the
+//                  concatenated adjacency of 32 queued vertices.
+//   2. sigma       exact uint64 path counts in topological order of the shortest-path DAG
+//                  (Kahn): a tight in-edge counter per vertex; a vertex joins the next
+//                  level when its last predecessor has pushed its count.  The predecessor
+//                  sets are implicit: v precedes w iff dist[v] + w(v,w) == dist[w], which
+//                  is exactly the reference's list after its clear-on-improve rule
+//                  (ExactBrandesBC.h:142-156).
+//   3. dependency  Kahn levels walked in reverse; each vertex pulls
+//                  sigma_v / sigma_w * (1 + delta_w) from its tight out-edges
+//                  (ExactBrandesBC.h:81) in adjacency order, so no atomics and a
+//                  deterministic sum; then BC[v] += card * delta_v (ExactBrandesBC.h:86-89,
+//                  ClusteredBrandesBC.h:151-155).
+//
+// Two schedules share this code through the Group template:
+//   BlockGroup  one source per thread block, per-source state in a global-memory slot
+//   WarpGroup   one source per warp, per-source state in shared memory (small segments)
+// and two precision forms through the Prec template:
+//   PrecF64     FP64 dependency arithmetic (the plain form)
+//   PrecDF32    FP32 double-float (two-sum compensated) dependency arithmetic; FP64 only
+//               for sigma ratios whose operands exceed 2^24 and for the BC reduction.
+//
+// Every loop is bounded: the distance pass stops after iter_cap rounds, the Kahn and
+// backward passes after n levels; a unit that hits a bound sets an error bit that the
+// host turns into a status code, and the state is still restored for the next unit.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace fbc {
+
+constexpr int32_t kInf = 0x7fffffff;
+constexpr unsigned kFull = 0xffffffffu;
+
+enum : int { kErrIter = 1, kErrSigma = 2, kErrQueue = 4 };
+
+// One CSR segment (device pointers).
+struct Seg {
+    const int32_t* rp;      // n+1 row offsets into adj
+    const int2* adj;        // packed (destination, weight) pairs, rows ascending
+    const int32_t* gid;     // n output indices (local -> BC index); null: out_base + local id
+    const int32_t* border;  // nb local ids of the border vertices (ascending global id)
+    int64_t out_base;
+    int32_t n;              // vertices
+    int32_t nb;             // border vertices (cluster segments), else 0
+    int32_t delta;          // bucket width of the near-far pass
+    int32_t pad;
+};
+
+// One source.
+struct Unit {
+    int32_t seg;
+    int32_t src;     // local id in the segment
+    double card;     // multiplicity of this source's dependency (pivot class cardinality)
+    int64_t bout;    // first border-output entry of this source, or -1
+};
+
+struct KParams {
+    const Seg* segs;
+    const Unit* units;
+    int64_t nunits;
+    double* bc;                  // BC accumulator (FP64)
+    double* bdist;               // border distances (0 when unreached)
+    unsigned long long* bsig;    // border path counts
+    unsigned long long* next_unit;
+    int* err;
+    char* ws;                    // global-memory slots (BlockGroup)
+    int64_t ws_stride;
+    int32_t ws_n;                // capacity (vertices) of one slot / one shared-memory state
+    int32_t iter_mult;           // distance-pass round cap = iter_mult * (n + 2)
+    int32_t* dbg_dist;           // debug dump of one unit (may be null)
+    unsigned long long* dbg_sig;
+    double* dbg_dlt;
+};
+
+// ----------------------------------------------------------------------------- groups
+struct BlockGroup {
+    static constexpr bool kShared = false;
+    __device__ static int rank() { return threadIdx.x; }
+    __device__ static int size() { return blockDim.x; }
+    __device__ static void sync() { __syncthreads(); }
+    __device__ static int warp() { return threadIdx.x >> 5; }
+    __device__ static int nwarps() { return blockDim.x >> 5; }
+};
+
+template <bool kSh>
+struct WarpGroup {
+    static constexpr bool kShared = kSh;
+    __device__ static int rank() { return threadIdx.x & 31; }
+    __device__ static int size() { return 32; }
+    __device__ static void sync() { __syncwarp(); }
+    __device__ static int warp() { return 0; }
+    __device__ static int nwarps() { return 1; }
+};
+
+// Loads of state that other threads modify with atomics: from L2 for global slots,
+// volatile for shared memory.
+template <bool kShared>
+__device__ __forceinline__ int ld_i32(const int* p) {
+    if constexpr (kShared) return *(const volatile int*)p;
+    else return __ldcg(p);
+}
+template <bool kShared>
+__device__ __forceinline__ unsigned long long ld_u64(const unsigned long long* p) {
+    if constexpr (kShared) return *(const volatile unsigned long long*)p;
+    else return __ldcg(p);
+}
+
+// ------------------------------------------------------------------------- precision
+struct PrecF64 {
+    using D = double;
+    struct Acc { double s; };
+    __device__ static Acc zero() { return {0.0}; }
+    // ExactBrandesBC.h:81: sigma[v] / sigma[w] * (1.0 + delta[w]), division first
+    __device__ static void add(Acc& a, unsigned long long sv, unsigned long long sw, D dw) {
+        a.s += (double)sv / (double)sw * (1.0 + dw);
+    }
+    __device__ static D store(const Acc& a) { return a.s; }
+    __device__ static Acc load(D d) { return {d}; }
+    __device__ static double value(const Acc& a) { return a.s; }
+};
+
+struct PrecDF32 {
+    using D = float2;  // (hi, lo) double-float
+    struct Acc { float hi, lo; };
+    __device__ static Acc zero() { return {0.f, 0.f}; }
+    // Knuth TwoSum and Dekker FastTwoSum / TwoProduct (via FMA), round-to-nearest intrinsics
+    // so that no contraction or reassociation changes them.
+    __device__ static void two_sum(float a, float b, float& s, float& e) {
+        s = __fadd_rn(a, b);
+        float bb = __fsub_rn(s, a);
+        e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+    }
+    __device__ static void fast_two_sum(float a, float b, float& s, float& e) {
+        s = __fadd_rn(a, b);
+        e = __fsub_rn(b, __fsub_rn(s, a));
+    }
+    __device__ static void add(Acc& a, unsigned long long sv, unsigned long long sw, D dw) {
+        // ratio r = sv / sw as a double-float
+        float rh, rl;
+        if (sv <= (1ull << 24) && sw <= (1ull << 24)) {
+            float x = (float)sv, y = (float)sw;   // exact
+            rh = __fdiv_rn(x, y);
+            rl = __fdiv_rn(__fmaf_rn(-rh, y, x), y);  // the remainder x - rh*y is exact
+        } else {
+            double rd = (double)sv / (double)sw;  // FP64 only above 2^24
+            rh = __double2float_rn(rd);
+            rl = __double2float_rn(rd - (double)rh);
+        }
+        // t = 1 + delta_w
+        float s, e, th, tl;
+        two_sum(1.0f, dw.x, s, e);
+        e = __fadd_rn(e, dw.y);
+        fast_two_sum(s, e, th, tl);
+        // c = r * t
+        float p = __fmul_rn(rh, th);
+        float pe = __fmaf_rn(rh, th, -p);
+        pe = __fadd_rn(pe, __fadd_rn(__fmul_rn(rh, tl), __fmul_rn(rl, th)));
+        float ch, cl;
+        fast_two_sum(p, pe, ch, cl);
+        // acc += c
+        two_sum(a.hi, ch, s, e);
+        e = __fadd_rn(e, __fadd_rn(a.lo, cl));
+        fast_two_sum(s, e, a.hi, a.lo);
+    }
+    __device__ static D store(const Acc& a) { return make_float2(a.hi, a.lo); }
+    __device__ static Acc load(D d) { return {d.x, d.y}; }
+    __device__ static double value(const Acc& a) { return (double)a.hi + (double)a.lo; }
+};
+
+// ------------------------------------------------------------------------ warp helpers
+// Visit every edge of up to 32 vertices (one per lane: row start e0, degree deg) with the
+// whole warp, edges of consecutive lanes back to back, so the adjacency reads of a round are
+// contiguous runs.  f(active, owner_lane, edge_index) is called by all 32 lanes each round.
+template <class F>
+__device__ __forceinline__ void warp_edges(int e0, int deg, F&& f) {
+    const int lane = threadIdx.x & 31;
+    int incl = deg;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int t = __shfl_up_sync(kFull, incl, o);
+        if (lane >= o) incl += t;
+    }
+    const int total = __shfl_sync(kFull, incl, 31);
+    const int excl = incl - deg;
+    for (int kb = 0; kb < total; kb += 32) {
+        const int k = kb + lane;
+        int j = 0;  // owner: the largest lane whose exclusive prefix is <= k
+#pragma unroll
+        for (int s = 16; s > 0; s >>= 1) {
+            int ex = __shfl_sync(kFull, excl, j + s);
+            if (ex <= k) j += s;
+        }
+        const int ev = __shfl_sync(kFull, e0, j) + (k - __shfl_sync(kFull, excl, j));
+        f(k < total, j, ev);
+    }
+}
+
+// Warp-aggregated append of x (where want) to q[0..cap), counter *cnt.
+__device__ __forceinline__ void warp_push(bool want, int x, int* q, int* cnt, int cap, int* err) {
+    const unsigned m = __ballot_sync(kFull, want);
+    if (!m) return;
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(m) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(cnt, __popc(m));
+    base = __shfl_sync(kFull, base, leader);
+    if (want) {
+        const int pos = base + __popc(m & ((1u << lane) - 1u));
+        if (pos < cap) q[pos] = x;
+        else atomicOr(err, kErrQueue);
+    }
+}
+
+// ----------------------------------------------------------------------- unit state
+// Per-source arrays (capacity cap vertices).  Invariant between units:
+// dist == kInf, sig == 0, cnt == 0 everywhere; nflag/fflag hold stamps < epoch.
+template <class Prec>
+struct State {
+    int* dist;
+    unsigned long long* sig;
+    typename Prec::D* dlt;
+    int* q[4];        // near0, near1, far0, far1 (cap+1 entries each)
+    unsigned* nflag;
+    unsigned* fflag;
+    int* cnt;
+};
+
+template <class Prec>
+__host__ __device__ inline int64_t state_bytes(int64_t cap) {
+    int64_t b = 0;
+    auto al = [](int64_t x) { return (x + 255) & ~int64_t(255); };
+    b += al(cap * 4);                               // dist
+    b += al(cap * 8);                               // sig
+    b += al(cap * (int64_t)sizeof(typename Prec::D));  // dlt
+    b += 4 * al((cap + 1) * 4);                     // queues
+    b += 2 * al(cap * 4);                           // flags
+    b += al(cap * 4);                               // cnt
+    return b;
+}
+
+template <class Prec>
+__device__ inline State<Prec> state_carve(char* base, int64_t cap) {
+    auto al = [](int64_t x) { return (x + 255) & ~int64_t(255); };
+    State<Prec> s;
+    char* p = base;
+    s.dist = (int*)p; p += al(cap * 4);
+    s.sig = (unsigned long long*)p; p += al(cap * 8);
+    s.dlt = (typename Prec::D*)p; p += al(cap * (int64_t)sizeof(typename Prec::D));
+    for (int i = 0; i < 4; ++i) { s.q[i] = (int*)p; p += al((cap + 1) * 4); }
+    s.nflag = (unsigned*)p; p += al(cap * 4);
+    s.fflag = (unsigned*)p; p += al(cap * 4);
+    s.cnt = (int*)p;
+    return s;
+}
+
+// Control words of one group (in shared memory).
+struct Ctl {
+    int ncnt[2];
+    int fcnt[2];
+    int dmin;
+    int ocnt;
+    int unit;
+    unsigned epoch;
+};
+
+// Fill a state with the invariant values (all cap entries).
+template <class G, class Prec>
+__device__ void state_init(const State<Prec>& s, int cap) {
+    for (int i = G::rank(); i < cap; i += G::size()) {
+        s.dist[i] = kInf;
+        s.sig[i] = 0ull;
+        s.nflag[i] = 0u;
+        s.fflag[i] = 0u;
+        s.cnt[i] = 0;
+    }
+    G::sync();
+}
+
+// ---------------------------------------------------------------------- one unit
+template <class G, class Prec>
+__device__ void run_unit(const KParams& P, const Unit& u, const State<Prec>& S, Ctl& C,
+                         unsigned& epoch, int cap) {
+    constexpr bool kSh = G::kShared;
+    const Seg sg = P.segs[u.seg];
+    const int n = sg.n;
+    const int* __restrict__ rp = sg.rp;
+    const int2* __restrict__ adj = sg.adj;
+    const int lane = threadIdx.x & 31;
+    const int src = u.src;
+    const int delta = sg.delta > 0 ? sg.delta : 1;
+    int bad = 0;
+
+    // Stamps must never repeat within the flag arrays' lifetime: renew them well before
+    // the 32-bit counter could wrap (the round cap bounds the stamps one unit uses).
+    const int64_t cap_rounds = (int64_t)P.iter_mult * ((int64_t)n + 2);
+    if ((int64_t)epoch + 2 * cap_rounds + 16 > 0x7fffffffLL) {
+        for (int i = G::rank(); i < cap; i += G::size()) { S.nflag[i] = 0u; S.fflag[i] = 0u; }
+        epoch = 1;
+        G::sync();
+    }
+
+    // ---------------------------------------------------------------- 1. distances
+    int T = delta;          // bucket threshold: near = tentative distance < T
+    int qs = 0, fs = 0;     // current near / far buffers
+    unsigned fgen = ++epoch;
+    if (G::rank() == 0) {
+        S.dist[src] = 0;
+        S.sig[src] = 1ull;
+        S.q[0][0] = src;
+        S.nflag[src] = epoch + 1;
+        C.ncnt[0] = 1;
+        C.ncnt[1] = 0;
+        C.fcnt[0] = 0;
+        C.fcnt[1] = 0;
+    }
+    G::sync();
+    int64_t rounds = 0;
+    for (;;) {
+        int ncur = C.ncnt[qs];
+        if (ncur > 0) {
+            if (++rounds > cap_rounds) { bad = kErrIter; break; }
+            const unsigned stamp = ++epoch;
+            const int* qc = S.q[qs];
+            int* qn = S.q[qs ^ 1];
+            int* qf = S.q[2 + fs];
+            for (int base = G::warp() * 32; base < ncur; base += G::nwarps() * 32) {
+                const int i = base + lane;
+                int e0 = 0, deg = 0, dv = 0;
+                if (i < ncur) {
+                    const int v = qc[i];
+                    dv = ld_i32<kSh>(S.dist + v);
+                    e0 = rp[v];
+                    deg = rp[v + 1] - e0;
+                }
+                warp_edges(e0, deg, [&](bool act, int j, int ev) {
+                    const int dvv = __shfl_sync(kFull, dv, j);
+                    bool pn = false, pf = false;
+                    int x = 0;
+                    if (act) {
+                        const int2 a = __ldg(adj + ev);
+                        x = a.x;
+                        const int nd = dvv + a.y;
+                        const int old = atomicMin(S.dist + x, nd);
+                        if (nd < old) {
+                            if (nd < T) pn = atomicExch(S.nflag + x, stamp) != stamp;
+                            else pf = atomicExch(S.fflag + x, fgen) != fgen;
+                        }
+                    }
+                    warp_push(pn, x, qn, &C.ncnt[qs ^ 1], cap + 1, P.err);
+                    warp_push(pf, x, qf, &C.fcnt[fs], cap + 1, P.err);
+                });
+            }
+            G::sync();
+            if (G::rank() == 0) C.ncnt[qs] = 0;
+            qs ^= 1;
+            G::sync();
+            continue;
+        }
+        // near queue empty: advance the threshold to the bucket of the closest far vertex
+        const int nfar = C.fcnt[fs];
+        if (nfar == 0) break;
+        if (++rounds > cap_rounds) { bad = kErrIter; break; }
+        if (G::rank() == 0) C.dmin = kInf;
+        G::sync();
+        const int* qf = S.q[2 + fs];
+        for (int i = G::rank(); i < nfar; i += G::size()) {
+            const int d = ld_i32<kSh>(S.dist + qf[i]);
+            if (d >= T) atomicMin(&C.dmin, d);
+        }
+        G::sync();
+        const int dmin = C.dmin;
+        if (dmin == kInf) break;  // every far entry was already settled
+        const int Told = T;
+        const int64_t tn = ((int64_t)dmin / delta + 1) * (int64_t)delta;
+        T = tn > (int64_t)kInf ? kInf : (int)tn;
+        const unsigned stamp = ++epoch;
+        fgen = ++epoch;
+        int* qn = S.q[qs];
+        int* qf2 = S.q[2 + (fs ^ 1)];
+        for (int base = G::warp() * 32; base < nfar; base += G::nwarps() * 32) {
+            const int i = base + lane;
+            bool pn = false, pf = false;
+            int x = 0;
+            if (i < nfar) {
+                x = qf[i];
+                const int d = ld_i32<kSh>(S.dist + x);
+                if (d >= Told) {
+                    if (d < T) pn = atomicExch(S.nflag + x, stamp) != stamp;
+                    else pf = atomicExch(S.fflag + x, fgen) != fgen;
+                }
+            }
+            warp_push(pn, x, qn, &C.ncnt[qs], cap + 1, P.err);
+            warp_push(pf, x, qf2, &C.fcnt[fs ^ 1], cap + 1, P.err);
+        }
+        G::sync();
+        if (G::rank() == 0) C.fcnt[fs] = 0;
+        fs ^= 1;
+        G::sync();
+    }
+    G::sync();
+
+    int* order = S.q[0];
+    int* lvl = S.q[1];
+    int nlev = 0;
+    int reached = 0;
+    if (!bad) {
+        // ---------------------------------------------------------- 2. sigma (Kahn)
+        // tight in-edge counts
+        for (int base = G::warp() * 32; base < n; base += G::nwarps() * 32) {
+            const int v = base + lane;
+            int e0 = 0, deg = 0, dv = kInf;
+            if (v < n) {
+                dv = ld_i32<kSh>(S.dist + v);
+                if (dv != kInf) {
+                    e0 = rp[v];
+                    deg = rp[v + 1] - e0;
+                }
+            }
+            warp_edges(e0, deg, [&](bool act, int j, int ev) {
+                const int dvv = __shfl_sync(kFull, dv, j);
+                if (act) {
+                    const int2 a = __ldg(adj + ev);
+                    if (dvv + a.y == ld_i32<kSh>(S.dist + a.x)) atomicAdd(S.cnt + a.x, 1);
+                }
+            });
+        }
+        if (G::rank() == 0) {
+            order[0] = src;
+            lvl[0] = 0;
+            C.ocnt = 1;
+        }
+        G::sync();
+        int lo = 0, hi = 1;
+        while (lo < hi) {
+            if (nlev >= n) { bad = kErrIter; break; }
+            for (int base = lo + G::warp() * 32; base < hi; base += G::nwarps() * 32) {
+                const int i = base + lane;
+                int e0 = 0, deg = 0, dv = 0;
+                unsigned long long sv = 0;
+                if (i < hi) {
+                    const int v = order[i];
+                    dv = ld_i32<kSh>(S.dist + v);
+                    sv = ld_u64<kSh>(S.sig + v);
+                    e0 = rp[v];
+                    deg = rp[v + 1] - e0;
+                }
+                warp_edges(e0, deg, [&](bool act, int j, int ev) {
+                    const int dvv = __shfl_sync(kFull, dv, j);
+                    const unsigned long long svv = __shfl_sync(kFull, sv, j);
+                    bool push = false;
+                    int x = 0;
+                    if (act) {
+                        const int2 a = __ldg(adj + ev);
+                        x = a.x;
+                        if (dvv + a.y == ld_i32<kSh>(S.dist + x)) {
+                            const unsigned long long old = atomicAdd(S.sig + x, svv);
+                            if (old + svv < old) atomicOr(P.err, kErrSigma);
+                            push = atomicSub(S.cnt + x, 1) == 1;
+                        }
+                    }
+                    warp_push(push, x, order, &C.ocnt, cap + 1, P.err);
+                });
+            }
+            G::sync();
+            ++nlev;
+            lo = hi;
+            hi = C.ocnt;
+            if (G::rank() == 0) lvl[nlev] = hi;
+            G::sync();
+        }
+        reached = hi;
+
+        // border (dist or 0 when unreached, sigma) of this source: DijkstraClusterEvaluator.h:166-177
+        if (u.bout >= 0) {
+            const int* bl = sg.border;
+            for (int j = G::rank(); j < sg.nb; j += G::size()) {
+                const int b = bl[j];
+                const int d = ld_i32<kSh>(S.dist + b);
+                P.bdist[u.bout + j] = d != kInf ? (double)d : 0.0;
+                P.bsig[u.bout + j] = ld_u64<kSh>(S.sig + b);
+            }
+        }
+    }
+    if (!bad) {
+        // ------------------------------------------------------- 3. dependency
+        const int* gid = sg.gid;
+        const double card = u.card;
+        for (int L = nlev - 1; L >= 0; --L) {
+            const int a0 = lvl[L], a1 = lvl[L + 1];
+            for (int i = a0 + G::rank(); i < a1; i += G::size()) {
+                const int v = order[i];
+                const int dv = ld_i32<kSh>(S.dist + v);
+                const unsigned long long sv = ld_u64<kSh>(S.sig + v);
+                typename Prec::Acc acc = Prec::zero();
+                const int e1 = rp[v + 1];
+                for (int e = rp[v]; e < e1; ++e) {
+                    const int2 a = __ldg(adj + e);
+                    if (dv + a.y == ld_i32<kSh>(S.dist + a.x)) {
+                        Prec::add(acc, sv, ld_u64<kSh>(S.sig + a.x), S.dlt[a.x]);
+                    }
+                }
+                S.dlt[v] = Prec::store(acc);
+                if (v != src) {
+                    const int64_t o = gid ? (int64_t)gid[v] : sg.out_base + v;
+                    atomicAdd(P.bc + o, card * Prec::value(acc));
+                }
+            }
+            G::sync();
+        }
+    }
+    (void)reached;
+    if (bad && G::rank() == 0) atomicOr(P.err, bad);
+    if (P.dbg_dist) {
+        for (int v = G::rank(); v < n; v += G::size()) {
+            const int d = ld_i32<kSh>(S.dist + v);
+            P.dbg_dist[v] = d != kInf ? d : -1;
+            P.dbg_sig[v] = ld_u64<kSh>(S.sig + v);
+            P.dbg_dlt[v] = d != kInf ? Prec::value(Prec::load(S.dlt[v])) : 0.0;
+        }
+        G::sync();
+    }
+
+    // ------------------------------------------------------------ restore invariant
+    for (int v = G::rank(); v < n; v += G::size()) {
+        S.dist[v] = kInf;
+        S.sig[v] = 0ull;
+        S.cnt[v] = 0;
+    }
+    G::sync();
+}
+
+// ------------------------------------------------------------------------- kernels
+// Block per source, state in a global-memory slot per block; blocks pull units from a
+// shared counter until none are left (persistent grid, sized by the host).
+template <class Prec>
+__global__ void __launch_bounds__(1024) brandes_block_kernel(KParams P) {
+    __shared__ Ctl C;
+    char* slot = P.ws + (int64_t)blockIdx.x * P.ws_stride;
+    unsigned* hdr = (unsigned*)slot;  // persistent stamp counter of this slot
+    State<Prec> S = state_carve<Prec>(slot + 256, P.ws_n);
+    unsigned epoch = hdr[0];
+    if (epoch == 0u) {  // fresh slot
+        state_init<BlockGroup, Prec>(S, P.ws_n);
+        epoch = 1u;
+    }
+    for (;;) {
+        if (threadIdx.x == 0) C.unit = (int)atomicAdd(P.next_unit, 1ull);
+        __syncthreads();
+        const int64_t ui = C.unit;
+        __syncthreads();
+        if (ui >= P.nunits) break;
+        const Unit u = P.units[ui];
+        run_unit<BlockGroup, Prec>(P, u, S, C, epoch, P.ws_n);
+    }
+    if (threadIdx.x == 0) hdr[0] = epoch;
+}
+
+// Warp per source.  kSh: state in shared memory (P.ws_n vertices per warp, dynamic shared
+// memory of blockDim/32 states); otherwise one global-memory slot per warp.
+template <class Prec, bool kSh>
+__global__ void __launch_bounds__(256) brandes_warp_kernel(KParams P) {
+    extern __shared__ __align__(256) char smem[];
+    __shared__ Ctl Cs[8];
+    const int w = threadIdx.x >> 5;
+    const int64_t per = state_bytes<Prec>(P.ws_n);
+    Ctl& C = Cs[w];
+    unsigned epoch;
+    unsigned* hdr = nullptr;
+    State<Prec> S;
+    if constexpr (kSh) {
+        S = state_carve<Prec>(smem + (int64_t)w * per, P.ws_n);
+        state_init<WarpGroup<kSh>, Prec>(S, P.ws_n);
+        epoch = 1u;
+    } else {
+        char* slot = P.ws + ((int64_t)blockIdx.x * (blockDim.x >> 5) + w) * P.ws_stride;
+        hdr = (unsigned*)slot;
+        S = state_carve<Prec>(slot + 256, P.ws_n);
+        epoch = hdr[0];
+        if (epoch == 0u) {
+            state_init<WarpGroup<kSh>, Prec>(S, P.ws_n);
+            epoch = 1u;
+        }
+    }
+    for (;;) {
+        int ui = 0;
+        if ((threadIdx.x & 31) == 0) ui = (int)atomicAdd(P.next_unit, 1ull);
+        ui = __shfl_sync(kFull, ui, 0);
+        if (ui >= P.nunits) break;
+        const Unit u = P.units[ui];
+        run_unit<WarpGroup<kSh>, Prec>(P, u, S, C, epoch, P.ws_n);
+    }
+    if (!kSh && (threadIdx.x & 31) == 0) hdr[0] = epoch;
+}
+
+}  // namespace fbc

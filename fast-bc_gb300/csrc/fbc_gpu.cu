@@ -1,0 +1,906 @@
+// libfbcgpu: C ABI over the GB300 Brandes engine (declarations and contracts in
+// include/fbc_gpu.h).  Host side: graph upload/validation, segment and unit planning,
+// workspace sizing, launches on the library stream, result download, status mapping.
+#include "fbc_gpu.h"
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "brandes_kernels.cuh"
+
+namespace {
+
+using fbc::KParams;
+using fbc::Seg;
+using fbc::Unit;
+
+thread_local std::string g_err;
+std::recursive_mutex g_mu;
+
+int fail(int code, const std::string& msg) {
+    g_err = msg;
+    return code;
+}
+
+#define FBC_CK(call)                                                                     \
+    do {                                                                                 \
+        cudaError_t e_ = (call);                                                         \
+        if (e_ != cudaSuccess) {                                                         \
+            int code_ = (e_ == cudaErrorMemoryAllocation) ? FBC_ERR_OOM : FBC_ERR_CUDA;  \
+            return fail(code_, std::string(#call) + ": " + cudaGetErrorString(e_));      \
+        }                                                                                \
+    } while (0)
+
+#define FBC_TRY(expr)          \
+    do {                       \
+        int rc_ = (expr);      \
+        if (rc_) return rc_;   \
+    } while (0)
+
+// Growable device buffer.
+struct DBuf {
+    void* p = nullptr;
+    size_t cap = 0;
+    cudaError_t ensure(size_t bytes, bool zero = false) {
+        if (p && bytes <= cap) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+        const size_t want = std::max<size_t>(bytes, 256);
+        cudaError_t e = cudaMalloc(&p, want);
+        if (e != cudaSuccess) {
+            p = nullptr;
+            return e;
+        }
+        cap = want;
+        if (zero) return cudaMemset(p, 0, want);
+        return cudaSuccess;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+    }
+    template <class T>
+    T* as() const {
+        return (T*)p;
+    }
+};
+
+struct Options {
+    int64_t delta = 0;          // bucket width; 0 = mean edge weight of the graph
+    int64_t block_threads = 256;
+    int64_t warp_max_n = 4096;  // batched: segments up to this size run one source per warp
+    int64_t iter_mult = 16;
+    int64_t ws_budget_mb = 0;   // 0 = 60% of the free device memory
+    int64_t warp_smem = 1;      // batched: warp state in shared memory when it fits
+};
+
+// A persistent workspace of equally sized slots.  Slot headers keep stamp counters, so a
+// workspace is reused across calls as long as its geometry still fits.
+struct Workspace {
+    DBuf buf;
+    int64_t stride = 0;
+    int64_t slots = 0;
+    int ws_n = -1;
+    int dsize = 0;
+};
+
+struct Ctx {
+    bool init = false;
+    int dev = 0;
+    int nsm = 0;
+    int smem_optin = 0;
+    cudaStream_t st = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    Options opt;
+    DBuf segs, units_b, units_w, crp, cadj, cgid, cbord, bc, bdist, bsig, ctr, dbg;
+    Workspace wsb, wsw;
+};
+Ctx g;
+
+double now_ms() {
+    return std::chrono::duration<double, std::milli>(
+               std::chrono::steady_clock::now().time_since_epoch())
+        .count();
+}
+
+}  // namespace
+
+struct fbc_graph_s {
+    int32_t n = 0;
+    int64_t m = 0;
+    int32_t maxw = 0;
+    double meanw = 1.0;
+    int32_t* d_rp = nullptr;
+    int2* d_adj = nullptr;
+    std::vector<int64_t> h_rp;
+    std::vector<int32_t> h_col;
+    std::vector<int32_t> h_w;
+};
+
+namespace {
+
+int check_init() {
+    if (!g.init) return fail(FBC_ERR_NOT_INIT, "fbc_gpu_init has not been called");
+    return FBC_OK;
+}
+
+// Validate a host CSR with double weights and build the device graph.
+int make_graph(int32_t n, std::vector<int64_t>&& rp, std::vector<int32_t>&& col, const double* w,
+               fbc_graph* out) {
+    if (n < 0) return fail(FBC_ERR_INVALID_ARG, "vertex count must be >= 0");
+    if (rp.size() != (size_t)n + 1 || rp[0] != 0) return fail(FBC_ERR_INVALID_ARG, "row_ptr[0] must be 0");
+    const int64_t m = rp[n];
+    if (m < 0 || m >= (int64_t)0x7fffffff) return fail(FBC_ERR_RANGE, "edge count outside [0, 2^31-1)");
+    std::vector<int32_t> wi((size_t)m);
+    int32_t maxw = 0;
+    double sumw = 0;
+    for (int32_t v = 0; v < n; ++v) {
+        if (rp[v + 1] < rp[v]) return fail(FBC_ERR_INVALID_ARG, "row_ptr is not monotone");
+        for (int64_t e = rp[v]; e < rp[v + 1]; ++e) {
+            if (col[e] < 0 || col[e] >= n)
+                return fail(FBC_ERR_INVALID_ARG,
+                            "edge destination out of range at vertex " + std::to_string(v));
+            if (e > rp[v] && col[e] <= col[e - 1])
+                return fail(FBC_ERR_INVALID_ARG,
+                            "CSR row not strictly ascending at vertex " + std::to_string(v));
+            const double x = w[e];
+            if (!(x > 0)) return fail(FBC_ERR_INVALID_ARG, "Edge weight must be greater than zero");
+            if (x != std::floor(x) || x > 2147483647.0)
+                return fail(FBC_ERR_RANGE, "edge weights must be integers below 2^31");
+            wi[e] = (int32_t)x;
+            maxw = std::max(maxw, wi[e]);
+            sumw += x;
+        }
+    }
+    if ((double)n * (double)maxw > 2147483646.0)
+        return fail(FBC_ERR_RANGE, "n * max_weight exceeds the int32 distance range");
+    auto* G = new fbc_graph_s();
+    G->n = n;
+    G->m = m;
+    G->maxw = maxw;
+    G->meanw = m ? sumw / (double)m : 1.0;
+    std::vector<int32_t> rp32((size_t)n + 1);
+    for (int32_t v = 0; v <= n; ++v) rp32[v] = (int32_t)rp[v];
+    std::vector<int2> adj((size_t)std::max<int64_t>(m, 1));
+    for (int64_t e = 0; e < m; ++e) adj[e] = make_int2(col[e], wi[e]);
+    cudaError_t e1 = cudaMalloc(&G->d_rp, sizeof(int32_t) * ((size_t)n + 1));
+    cudaError_t e2 = cudaMalloc(&G->d_adj, sizeof(int2) * adj.size());
+    if (e1 != cudaSuccess || e2 != cudaSuccess) {
+        if (e1 == cudaSuccess) cudaFree(G->d_rp);
+        if (e2 == cudaSuccess) cudaFree(G->d_adj);
+        delete G;
+        return fail(FBC_ERR_OOM, "device allocation of the graph failed");
+    }
+    cudaError_t e3 = cudaMemcpyAsync(G->d_rp, rp32.data(), sizeof(int32_t) * rp32.size(),
+                                     cudaMemcpyHostToDevice, g.st);
+    cudaError_t e4 = cudaMemcpyAsync(G->d_adj, adj.data(), sizeof(int2) * adj.size(),
+                                     cudaMemcpyHostToDevice, g.st);
+    cudaError_t e5 = cudaStreamSynchronize(g.st);
+    if (e3 != cudaSuccess || e4 != cudaSuccess || e5 != cudaSuccess) {
+        cudaFree(G->d_rp);
+        cudaFree(G->d_adj);
+        delete G;
+        return fail(FBC_ERR_CUDA, "graph upload failed");
+    }
+    G->h_rp = std::move(rp);
+    G->h_col = std::move(col);
+    G->h_w = std::move(wi);
+    *out = G;
+    return FBC_OK;
+}
+
+int delta_for(double meanw) {
+    if (g.opt.delta > 0) return (int)std::min<int64_t>(g.opt.delta, 0x3fffffff);
+    return std::max(1, (int)std::lround(meanw));
+}
+
+// A batch of work: segments + units, output sizes and debug pointers.
+struct Plan {
+    std::vector<Seg> segs;
+    std::vector<int64_t> seg_m;
+    std::vector<Unit> units;
+    int64_t bc_len = 0;
+    int64_t border_entries = 0;
+    int prec = FBC_PREC_FP64;
+    int sched = FBC_SCHED_PLAIN;
+    int32_t* dbg_dist = nullptr;
+    unsigned long long* dbg_sig = nullptr;
+    double* dbg_dlt = nullptr;
+};
+
+Seg whole_graph_seg(const fbc_graph_s* G, int64_t out_base) {
+    Seg s{};
+    s.rp = G->d_rp;
+    s.adj = G->d_adj;
+    s.gid = nullptr;
+    s.border = nullptr;
+    s.out_base = out_base;
+    s.n = G->n;
+    s.nb = 0;
+    s.delta = delta_for(G->meanw);
+    return s;
+}
+
+KParams base_params(const Plan& P) {
+    KParams K{};
+    K.segs = g.segs.as<Seg>();
+    K.bc = g.bc.as<double>();
+    K.bdist = g.bdist.as<double>();
+    K.bsig = g.bsig.as<unsigned long long>();
+    K.err = (int*)(g.ctr.as<unsigned long long>() + 2);
+    K.iter_mult = (int32_t)g.opt.iter_mult;
+    K.dbg_dist = P.dbg_dist;
+    K.dbg_sig = P.dbg_sig;
+    K.dbg_dlt = P.dbg_dlt;
+    return K;
+}
+
+// (Re)size a workspace for `slots` slots of `stride` bytes; reuse it when it already fits.
+int ensure_ws(Workspace& W, int64_t slots, int64_t stride, int ws_n, int dsize) {
+    if (W.buf.p && W.stride == stride && W.ws_n == ws_n && W.dsize == dsize && W.slots >= slots)
+        return FBC_OK;
+    W.buf.release();
+    FBC_CK(W.buf.ensure((size_t)(slots * stride), true));
+    W.stride = stride;
+    W.slots = slots;
+    W.ws_n = ws_n;
+    W.dsize = dsize;
+    return FBC_OK;
+}
+
+int64_t ws_budget() {
+    size_t freeb = 0, totalb = 0;
+    if (cudaMemGetInfo(&freeb, &totalb) != cudaSuccess) return (int64_t)1 << 30;
+    int64_t b = g.opt.ws_budget_mb > 0 ? g.opt.ws_budget_mb * (int64_t)1048576
+                                        : (int64_t)((double)freeb * 0.6);
+    return b + (int64_t)g.wsb.buf.cap + (int64_t)g.wsw.buf.cap;
+}
+
+template <class Prec>
+int launch_block(const Plan& P, const std::vector<Unit>& units, int ws_n, fbc_stats* st,
+                 int& launches) {
+    if (units.empty()) return FBC_OK;
+    const int64_t stride = 256 + ((fbc::state_bytes<Prec>(ws_n) + 255) & ~int64_t(255));
+    int threads = (int)std::min<int64_t>(std::max<int64_t>(g.opt.block_threads, 32), 1024);
+    threads = (threads / 32) * 32;
+    int bps = 0;
+    FBC_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, fbc::brandes_block_kernel<Prec>, threads, 0));
+    bps = std::max(bps, 1);
+    int64_t slots = std::min<int64_t>((int64_t)g.nsm * bps, (int64_t)units.size());
+    slots = std::max<int64_t>(1, std::min<int64_t>(slots, ws_budget() / stride));
+    FBC_TRY(ensure_ws(g.wsb, slots, stride, ws_n, (int)sizeof(typename Prec::D)));
+    FBC_CK(g.units_b.ensure(sizeof(Unit) * units.size()));
+    FBC_CK(cudaMemcpyAsync(g.units_b.p, units.data(), sizeof(Unit) * units.size(),
+                           cudaMemcpyHostToDevice, g.st));
+    if (st) st->h2d_bytes += (int64_t)(sizeof(Unit) * units.size());
+    KParams K = base_params(P);
+    K.units = g.units_b.as<Unit>();
+    K.nunits = (int64_t)units.size();
+    K.next_unit = g.ctr.as<unsigned long long>() + 0;
+    K.ws = g.wsb.buf.as<char>();
+    K.ws_stride = stride;
+    K.ws_n = ws_n;
+    fbc::brandes_block_kernel<Prec><<<(unsigned)slots, threads, 0, g.st>>>(K);
+    FBC_CK(cudaGetLastError());
+    ++launches;
+    if (st) st->slots = (int32_t)slots;
+    return FBC_OK;
+}
+
+template <class Prec>
+int launch_warp(const Plan& P, const std::vector<Unit>& units, int ws_n, fbc_stats* st,
+                int& launches) {
+    if (units.empty()) return FBC_OK;
+    const int64_t per = fbc::state_bytes<Prec>(ws_n);
+    const int64_t avail = (int64_t)g.smem_optin - (int64_t)sizeof(fbc::Ctl) * 8 - 1024;
+    const int64_t wpb_fit = per > 0 ? avail / per : 0;
+    FBC_CK(g.units_w.ensure(sizeof(Unit) * units.size()));
+    FBC_CK(cudaMemcpyAsync(g.units_w.p, units.data(), sizeof(Unit) * units.size(),
+                           cudaMemcpyHostToDevice, g.st));
+    if (st) st->h2d_bytes += (int64_t)(sizeof(Unit) * units.size());
+    KParams K = base_params(P);
+    K.units = g.units_w.as<Unit>();
+    K.nunits = (int64_t)units.size();
+    K.next_unit = g.ctr.as<unsigned long long>() + 1;
+    K.ws_n = ws_n;
+    if (g.opt.warp_smem && wpb_fit >= 1) {
+        const int wpb = (int)std::min<int64_t>(8, wpb_fit);
+        const size_t dyn = (size_t)(wpb * per);
+        auto kern = fbc::brandes_warp_kernel<Prec, true>;
+        FBC_CK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
+        int bps = 0;
+        FBC_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kern, 32 * wpb, dyn));
+        bps = std::max(bps, 1);
+        int64_t blocks = std::min<int64_t>((int64_t)g.nsm * bps,
+                                           ((int64_t)units.size() + wpb - 1) / wpb);
+        kern<<<(unsigned)blocks, 32 * wpb, dyn, g.st>>>(K);
+        FBC_CK(cudaGetLastError());
+    } else {
+        const int wpb = 8;
+        const int64_t stride = 256 + ((per + 255) & ~int64_t(255));
+        auto kern = fbc::brandes_warp_kernel<Prec, false>;
+        int bps = 0;
+        FBC_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kern, 32 * wpb, 0));
+        bps = std::max(bps, 1);
+        int64_t blocks = std::min<int64_t>((int64_t)g.nsm * bps,
+                                           ((int64_t)units.size() + wpb - 1) / wpb);
+        blocks = std::max<int64_t>(1, std::min<int64_t>(blocks, ws_budget() / (stride * wpb)));
+        FBC_TRY(ensure_ws(g.wsw, blocks * wpb, stride, ws_n, (int)sizeof(typename Prec::D)));
+        K.ws = g.wsw.buf.as<char>();
+        K.ws_stride = stride;
+        kern<<<(unsigned)blocks, 32 * wpb, 0, g.st>>>(K);
+        FBC_CK(cudaGetLastError());
+    }
+    ++launches;
+    return FBC_OK;
+}
+
+int map_err(int e) {
+    if (e & fbc::kErrQueue) return fail(FBC_ERR_QUEUE, "device work queue overflow");
+    if (e & fbc::kErrIter) return fail(FBC_ERR_ITER_LIMIT, "a device loop reached its iteration bound");
+    if (e & fbc::kErrSigma) return fail(FBC_ERR_SIGMA_OVERFLOW, "a shortest-path count exceeded 2^64-1");
+    return FBC_OK;
+}
+
+// Upload the plan, launch, wait, and check the device status.  Results stay on the device
+// (g.bc, g.bdist, g.bsig) for the caller to download.
+template <class Prec>
+int run_plan_t(Plan& P, fbc_stats* st) {
+    FBC_CK(g.segs.ensure(sizeof(Seg) * std::max<size_t>(P.segs.size(), 1)));
+    FBC_CK(cudaMemcpyAsync(g.segs.p, P.segs.data(), sizeof(Seg) * P.segs.size(),
+                           cudaMemcpyHostToDevice, g.st));
+    FBC_CK(g.bc.ensure(sizeof(double) * std::max<int64_t>(P.bc_len, 1)));
+    FBC_CK(cudaMemsetAsync(g.bc.p, 0, sizeof(double) * std::max<int64_t>(P.bc_len, 1), g.st));
+    FBC_CK(g.bdist.ensure(sizeof(double) * std::max<int64_t>(P.border_entries, 1)));
+    FBC_CK(g.bsig.ensure(sizeof(uint64_t) * std::max<int64_t>(P.border_entries, 1)));
+    FBC_CK(g.ctr.ensure(64));
+    FBC_CK(cudaMemsetAsync(g.ctr.p, 0, 64, g.st));
+    if (st) st->h2d_bytes += (int64_t)(sizeof(Seg) * P.segs.size());
+
+    // split units by schedule; biggest segments first (longest-processing-time order)
+    std::vector<Unit> ub, uw;
+    int nb_max = 0, nw_max = 0;
+    for (const Unit& u : P.units) {
+        const int n = P.segs[u.seg].n;
+        if (P.sched == FBC_SCHED_BATCHED && n <= g.opt.warp_max_n) {
+            uw.push_back(u);
+            nw_max = std::max(nw_max, n);
+        } else {
+            ub.push_back(u);
+            nb_max = std::max(nb_max, n);
+        }
+    }
+    auto by_size = [&](const Unit& a, const Unit& b) {
+        return P.segs[a.seg].n > P.segs[b.seg].n;
+    };
+    std::stable_sort(uw.begin(), uw.end(), by_size);
+    std::stable_sort(ub.begin(), ub.end(), by_size);
+
+    int launches = 0;
+    FBC_CK(cudaEventRecord(g.ev0, g.st));
+    FBC_TRY(launch_warp<Prec>(P, uw, nw_max, st, launches));
+    FBC_TRY(launch_block<Prec>(P, ub, nb_max, st, launches));
+    FBC_CK(cudaEventRecord(g.ev1, g.st));
+    int err = 0;
+    FBC_CK(cudaMemcpyAsync(&err, (char*)g.ctr.p + 16, sizeof(int), cudaMemcpyDeviceToHost, g.st));
+    FBC_CK(cudaStreamSynchronize(g.st));
+    if (st) {
+        float ms = 0.f;
+        FBC_CK(cudaEventElapsedTime(&ms, g.ev0, g.ev1));
+        st->kernel_ms += ms;
+        st->units += (int64_t)P.units.size();
+        double rel = 0;
+        for (const Unit& u : P.units) rel += (double)P.seg_m[u.seg];
+        st->relaxations += rel;
+        st->launches += launches;
+    }
+    return map_err(err);
+}
+
+int run_plan(Plan& P, fbc_stats* st) {
+    if (P.prec == FBC_PREC_FP32C) return run_plan_t<fbc::PrecDF32>(P, st);
+    if (P.prec == FBC_PREC_FP64) return run_plan_t<fbc::PrecF64>(P, st);
+    return fail(FBC_ERR_INVALID_ARG, "unknown precision");
+}
+
+int check_sched(int sched) {
+    if (sched != FBC_SCHED_PLAIN && sched != FBC_SCHED_BATCHED)
+        return fail(FBC_ERR_INVALID_ARG, "unknown schedule");
+    return FBC_OK;
+}
+
+int download_bc(double* out, int64_t len, bool accumulate, fbc_stats* st) {
+    if (!out || len <= 0) return FBC_OK;
+    std::vector<double> tmp;
+    double* dst = out;
+    if (accumulate) {
+        tmp.resize((size_t)len);
+        dst = tmp.data();
+    }
+    FBC_CK(cudaMemcpyAsync(dst, g.bc.p, sizeof(double) * (size_t)len, cudaMemcpyDeviceToHost, g.st));
+    FBC_CK(cudaStreamSynchronize(g.st));
+    if (st) st->d2h_bytes += (int64_t)(sizeof(double) * (size_t)len);
+    if (accumulate)
+        for (int64_t i = 0; i < len; ++i) out[i] += tmp[(size_t)i];
+    return FBC_OK;
+}
+
+// Border vertices of each cluster: a member with an in- or out-edge crossing the cluster
+// (SubGraph.h:70-135), ascending global id (the std::set order of SubGraph::borders).
+void compute_borders(const fbc_graph_s* G, int32_t nclusters, const int64_t* coff,
+                     const int32_t* cverts, const std::vector<int32_t>& cid,
+                     std::vector<int64_t>& boff, std::vector<int32_t>& bl) {
+    std::vector<char> isb((size_t)G->n, 0);
+    for (int32_t v = 0; v < G->n; ++v)
+        for (int64_t e = G->h_rp[v]; e < G->h_rp[v + 1]; ++e) {
+            const int32_t x = G->h_col[e];
+            if (cid[v] != cid[x]) {
+                isb[v] = 1;
+                isb[x] = 1;
+            }
+        }
+    boff.assign((size_t)nclusters + 1, 0);
+    bl.clear();
+    for (int32_t c = 0; c < nclusters; ++c) {
+        std::vector<int32_t> b;
+        for (int64_t i = coff[c]; i < coff[c + 1]; ++i)
+            if (isb[cverts[i]]) b.push_back(cverts[i]);
+        std::sort(b.begin(), b.end());
+        bl.insert(bl.end(), b.begin(), b.end());
+        boff[c + 1] = (int64_t)bl.size();
+    }
+}
+
+int cluster_ids(const fbc_graph_s* G, int32_t nclusters, const int64_t* coff, const int32_t* cverts,
+                std::vector<int32_t>& cid) {
+    if (nclusters < 0 || !coff || (nclusters > 0 && !cverts))
+        return fail(FBC_ERR_INVALID_ARG, "bad cluster arrays");
+    cid.assign((size_t)G->n, -1);
+    if (coff[0] != 0) return fail(FBC_ERR_INVALID_ARG, "cluster_off[0] must be 0");
+    for (int32_t c = 0; c < nclusters; ++c) {
+        if (coff[c + 1] < coff[c]) return fail(FBC_ERR_INVALID_ARG, "cluster_off is not monotone");
+        for (int64_t i = coff[c]; i < coff[c + 1]; ++i) {
+            const int32_t v = cverts[i];
+            if (v < 0 || v >= G->n) return fail(FBC_ERR_INVALID_ARG, "cluster vertex id out of range");
+            if (cid[v] != -1) return fail(FBC_ERR_INVALID_ARG, "vertex listed in two clusters or twice");
+            cid[v] = c;
+        }
+    }
+    return FBC_OK;
+}
+
+}  // namespace
+
+// ============================================================================ C ABI
+extern "C" {
+
+const char* fbc_last_error_string(void) { return g_err.c_str(); }
+
+int fbc_gpu_init(int device) {
+    std::lock_guard<std::recursive_mutex> lk(g_mu);
+    if (g.init) {
+        if (device == g.dev) return FBC_OK;
+        return fail(FBC_ERR_INVALID_ARG, "already initialised on another device");
+    }
+    int count = 0;
+    FBC_CK(cudaGetDeviceCount(&count));
+    if (device < 0 || device >= count) return fail(FBC_ERR_INVALID_ARG, "no such CUDA device");
+    FBC_CK(cudaSetDevice(device));
+    FBC_CK(cudaDeviceGetAttribute(&g.nsm, cudaDevAttrMultiProcessorCount, device));
+    FBC_CK(cudaDeviceGetAttribute(&g.smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device));
+    FBC_CK(cudaStreamCreateWithFlags(&g.st, cudaStreamNonBlocking));
+    FBC_CK(cudaEventCreate(&g.ev0));
+    FBC_CK(cudaEventCreate(&g.ev1));
+    g.dev = device;
+    g.init = true;
+    return FBC_OK;
+}
+
+int fbc_gpu_shutdown(void) {
+    std::lock_guard<std::recursive_mutex> lk(g_mu);
+    if (!g.init) return FBC_OK;
+    cudaStreamSynchronize(g.st);
+    for (DBuf* b : {&g.segs, &g.units_b, &g.units_w, &g.crp, &g.cadj, &g.cgid, &g.cbord, &g.bc,
+                    &g.bdist, &g.bsig, &g.ctr, &g.dbg})
+        b->release();
+    g.wsb.buf.release();
+    g.wsw.buf.release();
+    g.wsb = Workspace();
+    g.wsw = Workspace();
+    cudaEventDestroy(g.ev0);
+    cudaEventDestroy(g.ev1);
+    cudaStreamDestroy(g.st);
+    g.init = false;
+    return FBC_OK;
+}
+
+int fbc_set_option(const char* key, int64_t value) {
+    std::lock_guard<std::recursive_mutex> lk(g_mu);
+    if (!key) return fail(FBC_ERR_INVALID_ARG, "null option key");
+    std::string k(key);
+    if (k == "delta") g.opt.delta = std::max<int64_t>(0, value);
+    else if (k == "block_threads") g.opt.block_threads = std::max<int64_t>(32, std::min<int64_t>(1024, value));
+    else if (k == "warp_max_n") g.opt.warp_max_n = std::max<int64_t>(0, value);
+    else if (k == "iter_mult") g.opt.iter_mult = std::max<int64_t>(1, std::min<int64_t>(1 << 20, value));
+    else if (k == "ws_budget_mb") g.opt.ws_budget_mb = std::max<int64_t>(0, value);
+    else if (k == "warp_smem") g.opt.warp_smem = value ? 1 : 0;
+    else return fail(FBC_ERR_INVALID_ARG, "unknown option " + k);
+    return FBC_OK;
+}
+
+int fbc_get_option(const char* key, int64_t* value) {
+    std::lock_guard<std::recursive_mutex> lk(g_mu);
+    if (!key || !value) return fail(FBC_ERR_INVALID_ARG, "null argument");
+    std::string k(key);
+    if (k == "delta") *value = g.opt.delta;
+    else if (k == "block_threads") *value = g.opt.block_threads;
+    else if (k == "warp_max_n") *value = g.opt.warp_max_n;
+    else if (k == "iter_mult") *value = g.opt.iter_mult;
+    else if (k == "ws_budget_mb") *value = g.opt.ws_budget_mb;
+    else if (k == "warp_smem") *value = g.opt.warp_smem;
+    else return fail(FBC_ERR_INVALID_ARG, "unknown option " + k);
+    return FBC_OK;
+}
+
+int fbc_graph_upload(int32_t n, const int64_t* row_ptr, const int32_t* col, const double* w,
+                     fbc_graph* out) {
+    std::lock_guard<std::recursive_mutex> lk(g_mu);
+    FBC_TRY(check_init());
+    if (!out || !row_ptr || n < 0) return fail(FBC_ERR_INVALID_ARG, "null argument");
+    *out = nullptr;
+    std::vector<int64_t> rp(row_ptr, row_ptr + (size_t)n + 1);
+    const int64_t m = rp[n];
+    if (m < 0) return fail(FBC_ERR_INVALID_ARG, "negative edge count");
+    if (m > 0 && (!col || !w)) return fail(FBC_ERR_INVALID_ARG, "null edge arrays");
+    std::vector<int32_t> c(col, col + (size_t)m);
+    return make_graph(n, std::move(rp), std::move(c), w, out);
+}
+
+int fbc_graph_from_edges(int64_t count, const int32_t* src, const int32_t* dst, const double* w,
+                         fbc_graph* out) {
+    std::lock_guard<std::recursive_mutex> lk(g_mu);
+    FBC_TRY(check_init());
+    if (!out || count < 0 || (count > 0 && (!src || !dst || !w)))
+        return fail(FBC_ERR_INVALID_ARG, "null argument");
+    *out = nullptr;
+    int32_t maxs = -1;
+    for (int64_t i = 0; i < count; ++i) {
+        if (!(w[i] > 0)) return fail(FBC_ERR_INVALID_ARG, "Edge weight must be greater than zero");
+        if (src[i] < 0 || dst[i] < 0) return fail(FBC_ERR_INVALID_ARG, "negative vertex id");
+        maxs = std::max(maxs, src[i]);
+    }
+    const int32_t n = maxs + 1;
+    std::vector<int64_t> idx((size_t)count);
+    std::iota(idx.begin(), idx.end(), 0);
+    std::stable_sort(idx.begin(), idx.end(), [&](int64_t a, int64_t b) {
+        return src[a] != src[b] ? src[a] < src[b] : dst[a] < dst[b];
+    });
+    std::vector<int64_t> rp((size_t)n + 1, 0);
+    std::vector<int32_t> col;
+    std::vector<double> ww;
+    col.reserve((size_t)count);
+    ww.reserve((size_t)count);
+    int32_t ps = -1, pd = -1;
+    for (int64_t k = 0; k < count; ++k) {
+        const int64_t i = idx[(size_t)k];
+        if (dst[i] >= n)
+            return fail(FBC_ERR_INVALID_ARG, "destination id " + std::to_string(dst[i]) +
+                                                 " is not below 1 + max source id");
+        if (src[i] == ps && dst[i] == pd) {
+            ww.back() += w[i];  // DirectedWeightedGraph.h:154-155: repeated pair, weights summed
+        } else {
+            col.push_back(dst[i]);
+            ww.push_back(w[i]);
+            rp[(size_t)src[i] + 1]++;
+            ps = src[i];
+            pd = dst[i];
+        }
+    }
+    for (int32_t v = 0; v < n; ++v) rp[(size_t)v + 1] += rp[(size_t)v];
+    return make_graph(n, std::move(rp), std::move(col), ww.data(), out);
+}
+
+int fbc_graph_info(fbc_graph G, int32_t* n, int64_t* m) {
+    if (!G) return fail(FBC_ERR_INVALID_ARG, "null graph");
+    if (n) *n = G->n;
+    if (m) *m = G->m;
+    return FBC_OK;
+}
+
+int fbc_graph_download(fbc_graph G, int64_t* row_ptr, int32_t* col, double* w) {
+    if (!G) return fail(FBC_ERR_INVALID_ARG, "null graph");
+    if (row_ptr) std::copy(G->h_rp.begin(), G->h_rp.end(), row_ptr);
+    if (col) std::copy(G->h_col.begin(), G->h_col.end(), col);
+    if (w)
+        for (size_t e = 0; e < G->h_w.size(); ++e) w[e] = (double)G->h_w[e];
+    return FBC_OK;
+}
+
+int fbc_graph_free(fbc_graph G) {
+    std::lock_guard<std::recursive_mutex> lk(g_mu);
+    if (!G) return FBC_OK;
+    if (g.init) cudaStreamSynchronize(g.st);
+    cudaFree(G->d_rp);
+    cudaFree(G->d_adj);
+    delete G;
+    return FBC_OK;
+}
+
+int fbc_exact_bc(fbc_graph G, int precision, int sched, double* out_bc, fbc_stats* st) {
+    std::lock_guard<std::recursive_mutex> lk(g_mu);
+    FBC_TRY(check_init());
+    if (!G || (!out_bc && G->n > 0)) return fail(FBC_ERR_INVALID_ARG, "null argument");
+    FBC_TRY(check_sched(sched));
+    const double t0 = now_ms();
+    if (st) std::memset(st, 0, sizeof(*st));
+    Plan P;
+    P.prec = precision;
+    P.sched = sched;
+    P.segs.push_back(whole_graph_seg(G, 0));
+    P.seg_m.push_back(G->m);
+    for (int32_t s = 0; s < G->n; ++s) P.units.push_back(Unit{0, s, 1.0, -1});
+    P.bc_len = G->n;
+    FBC_TRY(run_plan(P, st));
+    FBC_TRY(download_bc(out_bc, G->n, false, st));
+    if (st) st->wall_ms = now_ms() - t0;
+    return FBC_OK;
+}
+
+int fbc_sssp_dependency_batch(fbc_graph G, int64_t count, const int32_t* sources,
+                              const double* cards, int precision, int sched, double* out_bc_accum,
+                              fbc_stats* st) {
+    std::lock_guard<std::recursive_mutex> lk(g_mu);
+    FBC_TRY(check_init());
+    if (!G || count < 0 || (count > 0 && !sources) || (!out_bc_accum && G->n > 0))
+        return fail(FBC_ERR_INVALID_ARG, "null argument");
+    FBC_TRY(check_sched(sched));
+    const double t0 = now_ms();
+    if (st) std::memset(st, 0, sizeof(*st));
+    Plan P;
+    P.prec = precision;
+    P.sched = sched;
+    P.segs.push_back(whole_graph_seg(G, 0));
+    P.seg_m.push_back(G->m);
+    for (int64_t i = 0; i < count; ++i) {
+        if (sources[i] < 0 || sources[i] >= G->n) return fail(FBC_ERR_INVALID_ARG, "source out of range");
+        P.units.push_back(Unit{0, sources[i], cards ? cards[i] : 1.0, -1});
+    }
+    P.bc_len = G->n;
+    if (st) st->h2d_bytes += count * (int64_t)(sizeof(int32_t) + sizeof(double));
+    FBC_TRY(run_plan(P, st));
+    FBC_TRY(download_bc(out_bc_accum, G->n, true, st));
+    if (st) st->wall_ms = now_ms() - t0;
+    return FBC_OK;
+}
+
+int fbc_single_source(fbc_graph G, int32_t source, int precision, double* out_dep, fbc_stats* st) {
+    std::lock_guard<std::recursive_mutex> lk(g_mu);
+    FBC_TRY(check_init());
+    if (!G || !out_dep) return fail(FBC_ERR_INVALID_ARG, "null argument");
+    std::fill(out_dep, out_dep + G->n, 0.0);
+    const double one = 1.0;
+    return fbc_sssp_dependency_batch(G, 1, &source, &one, precision, FBC_SCHED_PLAIN, out_dep, st);
+}
+
+int fbc_cluster_border_count(fbc_graph G, int32_t nclusters, const int64_t* coff,
+                             const int32_t* cverts, const int64_t* border_off, int64_t* out_nb,
+                             int64_t* out_entries) {
+    std::lock_guard<std::recursive_mutex> lk(g_mu);
+    if (!G) return fail(FBC_ERR_INVALID_ARG, "null graph");
+    std::vector<int32_t> cid;
+    FBC_TRY(cluster_ids(G, nclusters, coff, cverts, cid));
+    std::vector<int64_t> boff;
+    std::vector<int32_t> bl;
+    if (!border_off) {
+        compute_borders(G, nclusters, coff, cverts, cid, boff, bl);
+        border_off = boff.data();
+    }
+    int64_t nb = 0, ent = 0;
+    for (int32_t c = 0; c < nclusters; ++c) {
+        const int64_t b = border_off[c + 1] - border_off[c];
+        nb += b;
+        ent += b * (coff[c + 1] - coff[c]);
+    }
+    if (out_nb) *out_nb = nb;
+    if (out_entries) *out_entries = ent;
+    return FBC_OK;
+}
+
+int fbc_cluster_borders(fbc_graph G, int32_t nclusters, const int64_t* coff, const int32_t* cverts,
+                        int64_t* out_boff, int32_t* out_borders) {
+    std::lock_guard<std::recursive_mutex> lk(g_mu);
+    if (!G) return fail(FBC_ERR_INVALID_ARG, "null graph");
+    std::vector<int32_t> cid;
+    FBC_TRY(cluster_ids(G, nclusters, coff, cverts, cid));
+    std::vector<int64_t> boff;
+    std::vector<int32_t> bl;
+    compute_borders(G, nclusters, coff, cverts, cid, boff, bl);
+    if (out_boff) std::copy(boff.begin(), boff.end(), out_boff);
+    if (out_borders) std::copy(bl.begin(), bl.end(), out_borders);
+    return FBC_OK;
+}
+
+int fbc_cluster_eval_batch(fbc_graph G, int32_t nclusters, const int64_t* coff,
+                           const int32_t* cverts, const int64_t* border_off, const int32_t* borders,
+                           int precision, int sched, double* out_intra_bc, double* out_bdist,
+                           uint64_t* out_bsig, fbc_stats* st) {
+    std::lock_guard<std::recursive_mutex> lk(g_mu);
+    FBC_TRY(check_init());
+    if (!G) return fail(FBC_ERR_INVALID_ARG, "null graph");
+    FBC_TRY(check_sched(sched));
+    if (border_off && !borders) return fail(FBC_ERR_INVALID_ARG, "border_off without borders");
+    const double t0 = now_ms();
+    if (st) std::memset(st, 0, sizeof(*st));
+    std::vector<int32_t> cid;
+    FBC_TRY(cluster_ids(G, nclusters, coff, cverts, cid));
+    std::vector<int64_t> boff_v;
+    std::vector<int32_t> bl_v;
+    if (!border_off) {
+        compute_borders(G, nclusters, coff, cverts, cid, boff_v, bl_v);
+        border_off = boff_v.data();
+        borders = bl_v.data();
+    }
+    // local ids: position of each vertex in its cluster's list
+    std::vector<int32_t> lid((size_t)G->n, -1);
+    for (int32_t c = 0; c < nclusters; ++c)
+        for (int64_t i = coff[c]; i < coff[c + 1]; ++i) lid[cverts[i]] = (int32_t)(i - coff[c]);
+    // induced-subgraph CSRs (SubGraph::forwardStar keeps the intra-cluster edges)
+    const int64_t nv = coff[nclusters];
+    std::vector<int32_t> hrp;
+    std::vector<int2> hadj;
+    std::vector<int32_t> hbord;
+    std::vector<int64_t> rp_off((size_t)nclusters), adj_off((size_t)nclusters), b_off((size_t)nclusters);
+    std::vector<int64_t> seg_m((size_t)nclusters);
+    hrp.reserve((size_t)(nv + nclusters));
+    for (int32_t c = 0; c < nclusters; ++c) {
+        rp_off[c] = (int64_t)hrp.size();
+        adj_off[c] = (int64_t)hadj.size();
+        int32_t e = 0;
+        hrp.push_back(0);
+        for (int64_t i = coff[c]; i < coff[c + 1]; ++i) {
+            const int32_t v = cverts[i];
+            for (int64_t k = G->h_rp[v]; k < G->h_rp[v + 1]; ++k) {
+                const int32_t x = G->h_col[k];
+                if (cid[x] == c) {
+                    hadj.push_back(make_int2(lid[x], G->h_w[k]));
+                    ++e;
+                }
+            }
+            hrp.push_back(e);
+        }
+        seg_m[c] = e;
+        b_off[c] = (int64_t)hbord.size();
+        for (int64_t j = border_off[c]; j < border_off[c + 1]; ++j) {
+            const int32_t b = borders[j];
+            if (b < 0 || b >= G->n || cid[b] != c)
+                return fail(FBC_ERR_INVALID_ARG, "border vertex not in its cluster");
+            hbord.push_back(lid[b]);
+        }
+    }
+    FBC_CK(g.crp.ensure(sizeof(int32_t) * std::max<size_t>(hrp.size(), 1)));
+    FBC_CK(g.cadj.ensure(sizeof(int2) * std::max<size_t>(hadj.size(), 1)));
+    FBC_CK(g.cgid.ensure(sizeof(int32_t) * std::max<int64_t>(nv, 1)));
+    FBC_CK(g.cbord.ensure(sizeof(int32_t) * std::max<size_t>(hbord.size(), 1)));
+    if (!hrp.empty())
+        FBC_CK(cudaMemcpyAsync(g.crp.p, hrp.data(), sizeof(int32_t) * hrp.size(), cudaMemcpyHostToDevice, g.st));
+    if (!hadj.empty())
+        FBC_CK(cudaMemcpyAsync(g.cadj.p, hadj.data(), sizeof(int2) * hadj.size(), cudaMemcpyHostToDevice, g.st));
+    if (nv > 0)
+        FBC_CK(cudaMemcpyAsync(g.cgid.p, cverts, sizeof(int32_t) * (size_t)nv, cudaMemcpyHostToDevice, g.st));
+    if (!hbord.empty())
+        FBC_CK(cudaMemcpyAsync(g.cbord.p, hbord.data(), sizeof(int32_t) * hbord.size(), cudaMemcpyHostToDevice, g.st));
+    if (st)
+        st->h2d_bytes += (int64_t)(sizeof(int32_t) * (hrp.size() + (size_t)nv + hbord.size()) +
+                                   sizeof(int2) * hadj.size());
+    Plan P;
+    P.prec = precision;
+    P.sched = sched;
+    int64_t ent = 0;
+    const int dl = delta_for(G->meanw);
+    for (int32_t c = 0; c < nclusters; ++c) {
+        Seg s{};
+        s.rp = g.crp.as<int32_t>() + rp_off[c];
+        s.adj = g.cadj.as<int2>() + adj_off[c];
+        s.gid = g.cgid.as<int32_t>() + coff[c];
+        s.border = g.cbord.as<int32_t>() + b_off[c];
+        s.out_base = 0;
+        s.n = (int32_t)(coff[c + 1] - coff[c]);
+        s.nb = (int32_t)(border_off[c + 1] - border_off[c]);
+        s.delta = dl;
+        P.segs.push_back(s);
+        P.seg_m.push_back(seg_m[c]);
+        for (int32_t i = 0; i < s.n; ++i) P.units.push_back(Unit{c, i, 1.0, ent + (int64_t)i * s.nb});
+        ent += (int64_t)s.n * s.nb;
+    }
+    P.bc_len = G->n;
+    P.border_entries = ent;
+    FBC_TRY(run_plan(P, st));
+    FBC_TRY(download_bc(out_intra_bc, G->n, true, st));
+    if (ent > 0 && (out_bdist || out_bsig)) {
+        if (out_bdist)
+            FBC_CK(cudaMemcpyAsync(out_bdist, g.bdist.p, sizeof(double) * (size_t)ent, cudaMemcpyDeviceToHost, g.st));
+        if (out_bsig)
+            FBC_CK(cudaMemcpyAsync(out_bsig, g.bsig.p, sizeof(uint64_t) * (size_t)ent, cudaMemcpyDeviceToHost, g.st));
+        FBC_CK(cudaStreamSynchronize(g.st));
+        if (st) st->d2h_bytes += ent * (int64_t)((out_bdist ? 8 : 0) + (out_bsig ? 8 : 0));
+    }
+    if (st) st->wall_ms = now_ms() - t0;
+    return FBC_OK;
+}
+
+int fbc_multi_exact_bc(int32_t ngraphs, const fbc_graph* graphs, int precision, int sched,
+                       double* const* out_bc, fbc_stats* st) {
+    std::lock_guard<std::recursive_mutex> lk(g_mu);
+    FBC_TRY(check_init());
+    if (ngraphs < 0 || (ngraphs > 0 && (!graphs || !out_bc))) return fail(FBC_ERR_INVALID_ARG, "null argument");
+    FBC_TRY(check_sched(sched));
+    const double t0 = now_ms();
+    if (st) std::memset(st, 0, sizeof(*st));
+    Plan P;
+    P.prec = precision;
+    P.sched = sched;
+    std::vector<int64_t> base((size_t)ngraphs + 1, 0);
+    for (int32_t i = 0; i < ngraphs; ++i) {
+        if (!graphs[i]) return fail(FBC_ERR_INVALID_ARG, "null graph in batch");
+        P.segs.push_back(whole_graph_seg(graphs[i], base[i]));
+        P.seg_m.push_back(graphs[i]->m);
+        for (int32_t s = 0; s < graphs[i]->n; ++s) P.units.push_back(Unit{i, s, 1.0, -1});
+        base[i + 1] = base[i] + graphs[i]->n;
+    }
+    P.bc_len = base[ngraphs];
+    FBC_TRY(run_plan(P, st));
+    std::vector<double> all((size_t)std::max<int64_t>(P.bc_len, 1));
+    FBC_TRY(download_bc(all.data(), P.bc_len, false, st));
+    for (int32_t i = 0; i < ngraphs; ++i)
+        std::copy(all.begin() + base[i], all.begin() + base[i + 1], out_bc[i]);
+    if (st) st->wall_ms = now_ms() - t0;
+    return FBC_OK;
+}
+
+int fbc_sssp_debug(fbc_graph G, int32_t source, int32_t* out_dist, uint64_t* out_sigma,
+                   double* out_delta, int32_t* out_npred) {
+    std::lock_guard<std::recursive_mutex> lk(g_mu);
+    FBC_TRY(check_init());
+    if (!G || source < 0 || source >= G->n) return fail(FBC_ERR_INVALID_ARG, "bad graph or source");
+    const size_t n = (size_t)G->n;
+    FBC_CK(g.dbg.ensure(n * (4 + 8 + 8) + 512));
+    char* base = g.dbg.as<char>();
+    Plan P;
+    P.prec = FBC_PREC_FP64;
+    P.sched = FBC_SCHED_PLAIN;
+    P.segs.push_back(whole_graph_seg(G, 0));
+    P.seg_m.push_back(G->m);
+    P.units.push_back(Unit{0, source, 1.0, -1});
+    P.bc_len = G->n;
+    P.dbg_sig = (unsigned long long*)base;
+    P.dbg_dlt = (double*)(base + n * 8);
+    P.dbg_dist = (int32_t*)(base + n * 16);
+    FBC_TRY(run_plan(P, nullptr));
+    std::vector<int32_t> dist(n);
+    FBC_CK(cudaMemcpy(dist.data(), P.dbg_dist, 4 * n, cudaMemcpyDeviceToHost));
+    if (out_dist) std::copy(dist.begin(), dist.end(), out_dist);
+    if (out_sigma) FBC_CK(cudaMemcpy(out_sigma, P.dbg_sig, 8 * n, cudaMemcpyDeviceToHost));
+    if (out_delta) FBC_CK(cudaMemcpy(out_delta, P.dbg_dlt, 8 * n, cudaMemcpyDeviceToHost));
+    if (out_npred) {
+        std::fill(out_npred, out_npred + n, 0);
+        for (int32_t v = 0; v < G->n; ++v) {
+            if (dist[v] < 0) continue;
+            for (int64_t e = G->h_rp[v]; e < G->h_rp[v + 1]; ++e) {
+                const int32_t x = G->h_col[e];
+                if (dist[x] >= 0 && (int64_t)dist[v] + G->h_w[e] == dist[x]) out_npred[x]++;
+            }
+        }
+    }
+    return FBC_OK;
+}
+
+}  // extern "C"

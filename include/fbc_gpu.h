@@ -1,0 +1,145 @@
+/*
+ * fbc_gpu.h -- C ABI of the GB300 Brandes engine (libfbcgpu.so).
+ *
+ * The reference fast-bc has no C ABI or FFI: its hot path sits behind three C++
+ * template interfaces (V=int, W=double in the fbc CLI, main.cpp:25-31):
+ *   IBrandesBC<V,W>::computeBC               libfastbc/include/brandes/IBrandesBC.h:24
+ *   ISSBrandesBC<V,W>::singleSourceBrandes    libfastbc/include/brandes/ISSBrandesBC.h:26-28
+ *   IClusterEvaluator<V,W>::evaluateCluster   libfastbc/include/brandes/IClusterEvaluator.h:33-36
+ * Each entry point below is what an implementation of one of those interfaces calls
+ * (include/fastbc_gpu/*.hpp hold the C++ classes that implement them on top of this ABI).
+ * Plain pointers and sizes only; every call returns FBC_OK or an FBC_ERR_* status and
+ * never throws; fbc_last_error_string() describes the last failure of the calling thread.
+ * Calls are serialised by an internal mutex, so OpenMP worker threads may call in
+ * concurrently (the reference calls singleSourceBrandes from OMP workers,
+ * ClusteredBrandesBC.h:143-148).
+ *
+ * Graphs: directed, positive integer weights (the README's input contract), vertex ids
+ * 0..n-1, each CSR row sorted ascending without repeats (the std::map order of
+ * IGraph::forwardStar, IGraph.h:39).  Distances are int32 on the device: a graph whose
+ * (n-1)*max_weight reaches 2^31-1 is rejected with FBC_ERR_RANGE.
+ */
+#ifndef FBC_GPU_H
+#define FBC_GPU_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define FBC_OK 0
+#define FBC_ERR_INVALID_ARG 1   /* bad pointer/size/id, weight <= 0, unsorted row ...   */
+#define FBC_ERR_CUDA 2          /* a CUDA runtime call failed                           */
+#define FBC_ERR_OOM 3           /* device allocation failed                             */
+#define FBC_ERR_ITER_LIMIT 4    /* a device loop hit its iteration bound                */
+#define FBC_ERR_RANGE 5         /* weights or distances do not fit the int32 device form */
+#define FBC_ERR_SIGMA_OVERFLOW 6 /* a shortest-path count exceeded 2^64-1                */
+#define FBC_ERR_NOT_INIT 7      /* fbc_gpu_init has not been called                     */
+#define FBC_ERR_QUEUE 8         /* a device work queue overflowed (internal error)      */
+
+/* dependency precision (the "precision" form of the engine) */
+#define FBC_PREC_FP64 0   /* plain: FP64 dependency arithmetic                          */
+#define FBC_PREC_FP32C 1  /* FP32 double-float (two-sum compensated) dependency; FP64 only
+                             for sigma ratios above 2^24 and the cross-source BC sum     */
+
+/* schedule */
+#define FBC_SCHED_PLAIN 0    /* one source per thread block, per-source state in HBM     */
+#define FBC_SCHED_BATCHED 1  /* persistent mixed launch: one source per warp with state in
+                                shared memory for small segments, per block otherwise    */
+
+typedef struct fbc_graph_s* fbc_graph;
+
+/* Per-call measurements (all optional: pass NULL). */
+typedef struct {
+    double kernel_ms;        /* device time of the compute kernels, CUDA events on the
+                                library stream                                            */
+    double wall_ms;          /* host wall time of the whole call, copies included         */
+    int64_t h2d_bytes;       /* host->device bytes copied by the call                     */
+    int64_t d2h_bytes;       /* device->host bytes copied by the call                     */
+    int64_t units;           /* (segment, source) units processed                          */
+    double relaxations;      /* sum over units of the segment's edge count (TEPS numerator) */
+    int32_t launches;        /* kernels launched by the call                               */
+    int32_t slots;           /* concurrent block slots of the block-per-source kernel      */
+} fbc_stats;
+
+/* Library lifetime.  fbc_gpu_init selects the device and creates the library stream. */
+int fbc_gpu_init(int device);
+int fbc_gpu_shutdown(void);
+const char* fbc_last_error_string(void);
+
+/* Tuning knobs (the autotuner sets these): "delta" bucket width (0 = automatic),
+ * "block_threads", "warp_max_n" (largest segment run warp-per-source), "iter_mult",
+ * "ws_budget_mb".  Unknown key -> FBC_ERR_INVALID_ARG. */
+int fbc_set_option(const char* key, int64_t value);
+int fbc_get_option(const char* key, int64_t* value);
+
+/* Device graph from CSR (row_ptr[n+1], col[m], w[m], double weights as in W=double).
+ * Replaces building a DirectedWeightedGraph for the GPU (DirectedWeightedGraph.h:67-170). */
+int fbc_graph_upload(int32_t n, const int64_t* row_ptr, const int32_t* col, const double* w,
+                     fbc_graph* out);
+
+/* Device graph from an edge list with the reference parser's rules
+ * (DirectedWeightedGraph.h:67-96, 136-170): weight <= 0 rejected, repeated (src,dst)
+ * pairs have their weights summed, n = 1 + max source id (a destination id >= n, which
+ * is undefined behaviour in the reference, is rejected). */
+int fbc_graph_from_edges(int64_t count, const int32_t* src, const int32_t* dst, const double* w,
+                         fbc_graph* out);
+
+int fbc_graph_info(fbc_graph g, int32_t* n, int64_t* m);
+/* Download the CSR (row_ptr[n+1], col[m], w[m]); any pointer may be NULL. */
+int fbc_graph_download(fbc_graph g, int64_t* row_ptr, int32_t* col, double* w);
+int fbc_graph_free(fbc_graph g);
+
+/* Exact BC over every source (ExactBrandesBC::computeBC, ExactBrandesBC.h:45-95).
+ * out_bc[n] is overwritten. */
+int fbc_exact_bc(fbc_graph g, int precision, int sched, double* out_bc, fbc_stats* st);
+
+/* One source's dependency vector, dep[source] = 0
+ * (DijkstraSSBrandesBC::singleSourceBrandes, DijkstraSSBrandesBC.h:45-81).  out_dep[n]. */
+int fbc_single_source(fbc_graph g, int32_t source, int precision, double* out_dep,
+                      fbc_stats* st);
+
+/* Batched pivot dependencies: out_bc_accum[v] += sum_p cards[p] * dep_p[v]
+ * (the pivot loop of ClusteredBrandesBC.h:141-155; cards may be NULL for all-ones). */
+int fbc_sssp_dependency_batch(fbc_graph g, int64_t count, const int32_t* sources,
+                              const double* cards, int precision, int sched,
+                              double* out_bc_accum, fbc_stats* st);
+
+/* Batched cluster evaluation (DijkstraClusterEvaluator::evaluateCluster,
+ * DijkstraClusterEvaluator.h:50-180) for nclusters clusters at once.  Cluster c holds
+ * cluster_vertices[cluster_off[c] .. cluster_off[c+1]); each of them is a source over the
+ * cluster's induced subgraph (SubGraph::forwardStar, SubGraph.h:165-176).
+ * Borders: border_off/borders give each cluster's border vertices in ascending id order
+ * (SubGraph::borders); pass border_off = NULL to have them computed (a vertex with an in-
+ * or out-edge crossing the cluster, SubGraph.h:70-135).
+ * Outputs: out_intra_bc[n] += intra-cluster BC (global ids); for the i-th vertex of
+ * cluster c and its j-th border: out_border_dist[E_c + i*nb_c + j] (0 when unreached) and
+ * out_border_sigma[...], E_c = sum_{c'<c} n_c' * nb_c'.  The caller sizes the border outputs
+ * with fbc_cluster_border_count; either may be NULL. */
+int fbc_cluster_border_count(fbc_graph g, int32_t nclusters, const int64_t* cluster_off,
+                             const int32_t* cluster_vertices, const int64_t* border_off,
+                             int64_t* out_nborders_total, int64_t* out_entries);
+int fbc_cluster_borders(fbc_graph g, int32_t nclusters, const int64_t* cluster_off,
+                        const int32_t* cluster_vertices, int64_t* out_border_off,
+                        int32_t* out_borders);
+int fbc_cluster_eval_batch(fbc_graph g, int32_t nclusters, const int64_t* cluster_off,
+                           const int32_t* cluster_vertices, const int64_t* border_off,
+                           const int32_t* borders, int precision, int sched,
+                           double* out_intra_bc, double* out_border_dist,
+                           uint64_t* out_border_sigma, fbc_stats* st);
+
+/* Exact BC of several independent graphs in one persistent launch.  out_bc[g] has
+ * n_g entries. */
+int fbc_multi_exact_bc(int32_t ngraphs, const fbc_graph* graphs, int precision, int sched,
+                       double* const* out_bc, fbc_stats* st);
+
+/* Debug dump of one source: dist (-1 when unreached), sigma, delta (FP64 form) and the
+ * number of shortest-path predecessors of each vertex; any output may be NULL. */
+int fbc_sssp_debug(fbc_graph g, int32_t source, int32_t* out_dist, uint64_t* out_sigma,
+                   double* out_delta, int32_t* out_npred);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

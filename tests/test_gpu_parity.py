@@ -1,0 +1,207 @@
+"""GPU parity through the C ABI (libfbcgpu.so) against the CPU oracle.
+
+Bars (the engine's contract):
+  * distances and shortest-path counts bit-exact; predecessor sets equal (the oracle's
+    predecessor lists, compared as sets with the tight in-edges implied by the GPU distances);
+  * BC within 1e-9 relative of the FP64 oracle in the plain (FP64) form;
+  * BC within 1e-6 relative in the FP32-compensated form.
+"""
+import numpy as np
+import pytest
+
+import graphs
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+TOL_FP64 = 1e-9
+TOL_FP32C = 1e-6
+
+
+def rel_err(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    scale = np.maximum(np.abs(b), 1e-300)
+    d = np.abs(a - b)
+    d[(a == 0) & (b == 0)] = 0
+    return float(np.max(d / scale)) if d.size else 0.0
+
+
+def dwg():
+    import os
+    from conftest import GOLDEN
+
+    a = np.loadtxt(os.path.join(GOLDEN, "DWGtext.txt"), ndmin=2)
+    return a[:, 0].astype(np.int32), a[:, 1].astype(np.int32), a[:, 2]
+
+
+def to_csr(src, dst, w):
+    n = int(src.max()) + 1
+    order = np.lexsort((dst, src))
+    s, d, ww = src[order], dst[order], w[order]
+    rp = np.zeros(n + 1, np.int64)
+    np.cumsum(np.bincount(s, minlength=n), out=rp[1:])
+    return oracle.CSR(rp, d, ww)
+
+
+def check_source(fg, g, og, src):
+    dist, sig, dlt, npred = fg.sssp_debug(g, src)
+    od, osg, odl, order, preds = oracle.sssp_dump(og, src)
+    gd = np.where(dist < 0, np.inf, dist.astype(np.float64))
+    assert np.array_equal(gd, od), f"dist differs for source {src}"
+    assert np.array_equal(sig.astype(np.float64), osg), f"sigma differs for source {src}"
+    assert np.array_equal(npred, np.array([len(p) for p in preds])), f"pred count differs, source {src}"
+    # predecessor sets: oracle's lists vs tight in-edges implied by the GPU distances
+    rp, col, w = og.rp, og.col, og.w
+    for v in order[: min(len(order), 400)]:
+        for e in range(rp[v], rp[v + 1]):
+            x = col[e]
+            if gd[v] + w[e] == gd[x]:
+                assert v in set(preds[x].tolist())
+    reached = od < np.inf
+    assert rel_err(dlt[reached], odl[reached]) <= TOL_FP64
+
+
+def test_dwg_sssp_bit_exact(fg):
+    s, d, w = dwg()
+    g = fg.Graph.from_edges(s, d, w)
+    og = to_csr(s, d, w)
+    assert g.n == 9 and g.m == 16
+    for src in range(9):
+        check_source(fg, g, og, src)
+
+
+def test_dwg_exact_bc_matches_reference_golden(fg):
+    """Full-graph exact BC of the reference's test graph (reference ExactBrandesBC, FP64)."""
+    s, d, w = dwg()
+    g = fg.Graph.from_edges(s, d, w)
+    golden = np.array([2, 4.333333333333333, 1.3333333333333333, 7.333333333333333,
+                       7.6666666666666661, 7.333333333333333, 0, 0, 2])
+    for prec, tol in ((fg.FP64, TOL_FP64), (fg.FP32C, TOL_FP32C)):
+        for sched in (fg.PLAIN, fg.BATCHED):
+            bc = fg.exact_bc(g, prec, sched)
+            assert rel_err(bc, golden) <= tol
+
+
+def test_dwg_subgraph_known_answers(fg):
+    """ExactBrandesBC.cpp:31-35 and DijkstraClusterEvaluator.cpp:73-109 on SubGraph {0..4}."""
+    s, d, w = dwg()
+    g = fg.Graph.from_edges(s, d, w)
+    cs = fg.ClusterSet.from_lists([[0, 1, 2, 3, 4]])
+    for prec in (fg.FP64, fg.FP32C):
+        for sched in (fg.PLAIN, fg.BATCHED):
+            ev = fg.cluster_eval_batch(g, cs, prec, sched)
+            assert np.array_equal(ev.intra_bc, [2, 2, 0.5, 1, 0, 0, 0, 0, 0])
+            assert list(ev.clusters.borders) == [3, 4]
+            want = {0: ([5, 7], [1, 2]), 1: ([1, 4], [1, 1]), 2: ([8, 4], [1, 1]),
+                    3: ([0, 3], [1, 1]), 4: ([0, 0], [0, 1])}
+            for i, (lens, cnts) in want.items():
+                L, Cn = ev.vertex_info(0, i)
+                assert list(L) == lens and list(Cn) == cnts
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+@pytest.mark.parametrize("sched", [0, 1])
+def test_grid32_exact(fg, prec, sched):
+    el = graphs.WORKLOADS["grid32"]()
+    og = oracle.CSR.from_edgelist(el)
+    ref = oracle.exact_bc(og)
+    g = fg.Graph.from_edgelist(el)
+    bc = fg.exact_bc(g, prec, sched)
+    assert rel_err(bc, ref) <= (TOL_FP64 if prec == 0 else TOL_FP32C)
+
+
+def test_grid32_sources_bit_exact(fg):
+    el = graphs.WORKLOADS["grid32"]()
+    og = oracle.CSR.from_edgelist(el)
+    g = fg.Graph.from_edgelist(el)
+    for src in (0, 1, 31, 500, 1023):
+        check_source(fg, g, og, src)
+
+
+def test_grid256_sources_bit_exact(fg):
+    el = graphs.WORKLOADS["grid256"]()
+    og = oracle.CSR.from_edgelist(el)
+    g = fg.Graph.from_edgelist(el)
+    for src in (0, 12345, 65535):
+        check_source(fg, g, og, src)
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_grid256_pivot_batch(fg, prec):
+    el = graphs.WORKLOADS["grid256"]()
+    og = oracle.CSR.from_edgelist(el)
+    g = fg.Graph.from_edgelist(el)
+    rng = np.random.default_rng(3)
+    piv = rng.choice(el.n, 24, replace=False).astype(np.int32)
+    cards = rng.integers(1, 9, piv.size).astype(np.float64)
+    ref = oracle.pivot_batch(og, piv, cards)
+    for sched in (fg.PLAIN, fg.BATCHED):
+        got = fg.dependency_batch(g, piv, cards, prec, sched)
+        assert rel_err(got, ref) <= (TOL_FP64 if prec == 0 else TOL_FP32C)
+
+
+def test_rgg_small_exact(fg):
+    el = graphs.rgg_knn(1500, seed=11)
+    og = oracle.CSR.from_edgelist(el)
+    ref = oracle.exact_bc(og)
+    g = fg.Graph.from_edgelist(el)
+    for prec, tol in ((fg.FP64, TOL_FP64), (fg.FP32C, TOL_FP32C)):
+        for sched in (fg.PLAIN, fg.BATCHED):
+            assert rel_err(fg.exact_bc(g, prec, sched), ref) <= tol
+    for src in (0, 700, 1499):
+        check_source(fg, g, og, src)
+
+
+def test_multi_graph_batch(fg):
+    els = [graphs.rgg_knn(n, seed=5, gid=i) for i, n in enumerate([1024, 1300, 2100])]
+    gs = [fg.Graph.from_edgelist(e) for e in els]
+    for prec, tol in ((fg.FP64, TOL_FP64), (fg.FP32C, TOL_FP32C)):
+        outs = fg.multi_exact_bc(gs, prec, fg.BATCHED)
+        for e, o in zip(els, outs):
+            assert rel_err(o, oracle.exact_bc(oracle.CSR.from_edgelist(e))) <= tol
+
+
+def test_cluster_eval_grid(fg):
+    """Tile a 64x64 grid into 16 square clusters; compare intra BC and border (dist, sigma)."""
+    el = graphs.road_grid(64, 64, seed=9)
+    og = oracle.CSR.from_edgelist(el)
+    g = fg.Graph.from_edgelist(el)
+    ids = np.arange(el.n)
+    tile = (ids // 64) // 16 * 4 + (ids % 64) // 16
+    clusters = [ids[tile == t].astype(np.int32) for t in range(16)]
+    cs = fg.ClusterSet.from_lists(clusters).with_borders(g)
+    ref_bc = np.zeros(el.n)
+    refs = []
+    for c, vs in enumerate(clusters):
+        b = cs.borders[cs.boff[c]:cs.boff[c + 1]]
+        _, bd, bs = oracle.cluster_eval(og, vs, b, ref_bc)
+        refs.append((bd, bs))
+    for prec, tol in ((fg.FP64, TOL_FP64), (fg.FP32C, TOL_FP32C)):
+        for sched in (fg.PLAIN, fg.BATCHED):
+            ev = fg.cluster_eval_batch(g, cs, prec, sched)
+            assert rel_err(ev.intra_bc, ref_bc) <= tol
+            for c, (bd, bs) in enumerate(refs):
+                for i in range(len(clusters[c])):
+                    L, Cn = ev.vertex_info(c, i)
+                    assert np.array_equal(L, bd[i]) and np.array_equal(Cn.astype(np.float64), bs[i])
+
+
+def test_invalid_inputs_raise(fg):
+    with pytest.raises(fg.FbcError) as e:
+        fg.Graph.from_edges(np.array([0, 1], np.int32), np.array([1, 0], np.int32), np.array([1.0, 0.0]))
+    assert e.value.code == fg.FBC_ERR_INVALID_ARG
+    with pytest.raises(fg.FbcError):
+        fg.Graph.from_edges(np.array([0], np.int32), np.array([5], np.int32), np.array([1.0]))
+    with pytest.raises(fg.FbcError) as e:
+        fg.Graph.from_edges(np.array([0, 1], np.int32), np.array([1, 0], np.int32), np.array([1.5, 1.0]))
+    assert e.value.code == fg.FBC_ERR_RANGE
+
+
+def test_duplicate_edges_summed(fg):
+    """DirectedWeightedGraph.h:154-165: a repeated pair has its weights summed."""
+    g = fg.Graph.from_edges(np.array([0, 0, 1, 0, 2], np.int32), np.array([1, 2, 2, 1, 0], np.int32),
+                            np.array([2.0, 5.0, 1.0, 2.0, 1.0]))
+    rp, col, w = g.csr()
+    assert g.n == 3 and g.m == 4
+    assert list(col[rp[0]:rp[1]]) == [1, 2] and list(w[rp[0]:rp[1]]) == [4.0, 5.0]

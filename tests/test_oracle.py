@@ -1,0 +1,81 @@
+"""The CPU oracle pinned to the reference's known answers (CPU only)."""
+import os
+
+import numpy as np
+import pytest
+
+import graphs
+import oracle
+from conftest import GOLDEN
+
+
+def dwg_csr():
+    a = np.loadtxt(os.path.join(GOLDEN, "DWGtext.txt"), ndmin=2)
+    s, d, w = a[:, 0].astype(np.int32), a[:, 1].astype(np.int32), a[:, 2]
+    n = int(s.max()) + 1
+    o = np.lexsort((d, s))
+    rp = np.zeros(n + 1, np.int64)
+    np.cumsum(np.bincount(s[o], minlength=n), out=rp[1:])
+    return oracle.CSR(rp, d[o], w[o])
+
+
+def sub_csr(g, verts):
+    """Induced subgraph on ids 0..k-1 (the reference's SubGraph {0..4} test fixture)."""
+    k = len(verts)
+    rows, cols, ws = [], [], []
+    rp = [0]
+    for v in verts:
+        for e in range(g.rp[v], g.rp[v + 1]):
+            if g.col[e] < k:
+                cols.append(g.col[e]); ws.append(g.w[e])
+        rp.append(len(cols))
+    return oracle.CSR(np.array(rp), np.array(cols, np.int32), np.array(ws))
+
+
+def test_exact_subgraph_known_answer():
+    """libfastbc/test/brandes/ExactBrandesBC.cpp:31-35."""
+    bc = oracle.exact_bc(sub_csr(dwg_csr(), [0, 1, 2, 3, 4]))
+    assert list(bc) == [2.0, 2.0, 0.5, 1.0, 0.0]
+
+
+def test_cluster_evaluator_known_answers():
+    """libfastbc/test/brandes/DijkstraClusterEvaluator.cpp:73-109."""
+    g = dwg_csr()
+    bc, bd, bs = oracle.cluster_eval(g, [0, 1, 2, 3, 4], [3, 4])
+    assert list(bc) == [2, 2, 0.5, 1, 0, 0, 0, 0, 0]
+    want_len = [[5, 7], [1, 4], [8, 4], [0, 3], [0, 0]]
+    want_cnt = [[1, 2], [1, 1], [1, 1], [1, 1], [0, 1]]
+    assert bd.tolist() == want_len and bs.tolist() == want_cnt
+
+
+def test_full_dwg_exact_golden():
+    """Reference ExactBrandesBC<int,double> on the whole test graph (golden from the reference)."""
+    bc = oracle.exact_bc(dwg_csr())
+    golden = [2, 4.333333333333333, 1.3333333333333333, 7.333333333333333,
+              7.6666666666666661, 7.333333333333333, 0, 0, 2]
+    assert bc.tolist() == golden
+
+
+def test_grid32_exact_matches_reference_bitwise():
+    path = os.path.join(GOLDEN, "grid32_exact_bc.txt")
+    golden = np.loadtxt(path)
+    bc = oracle.exact_bc(oracle.CSR.from_edgelist(graphs.WORKLOADS["grid32"]()))
+    assert np.array_equal(bc, golden)
+
+
+def test_grid32_threads_agree():
+    g = oracle.CSR.from_edgelist(graphs.WORKLOADS["grid32"]())
+    a = oracle.exact_bc(g, 1)
+    b = oracle.exact_bc(g, 4)
+    assert np.max(np.abs(a - b) / np.maximum(a, 1e-300)) < 1e-12
+
+
+def test_single_source_and_dump_consistent():
+    g = oracle.CSR.from_edgelist(graphs.WORKLOADS["grid32"]())
+    dep = oracle.single_source(g, 77)
+    dist, sig, dlt, order, preds = oracle.sssp_dump(g, 77)
+    assert dep[77] == 0
+    assert np.array_equal(dep[np.arange(g.n) != 77], dlt[np.arange(g.n) != 77])
+    assert order[0] == 77 and np.all(np.diff(dist[order]) >= 0)
+    for v in range(g.n):
+        assert sig[v] == sum(sig[p] for p in preds[v]) or v == 77
