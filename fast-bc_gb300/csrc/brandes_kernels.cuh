@@ -472,10 +472,10 @@ __device__ void run_unit(const KParams& P, const Unit& u, const State<Prec>& S, 
                 });
             }
             G::sync();
-            ++nlev;
+            ++nlev;                                // level nlev-1 = order[lo, hi) is done
+            if (G::rank() == 0) lvl[nlev] = hi;    // lvl[L] = first entry of level L
             lo = hi;
             hi = C.ocnt;
-            if (G::rank() == 0) lvl[nlev] = hi;
             G::sync();
         }
         reached = hi;

@@ -99,7 +99,7 @@ struct Ctx {
     int nsm = 0;
     int smem_optin = 0;
     cudaStream_t st = nullptr;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, evm = nullptr;
     Options opt;
     DBuf segs, units_b, units_w, crp, cadj, cgid, cbord, bc, bdist, bsig, ctr, dbg;
     Workspace wsb, wsw;
@@ -388,15 +388,24 @@ int run_plan_t(Plan& P, fbc_stats* st) {
     int launches = 0;
     FBC_CK(cudaEventRecord(g.ev0, g.st));
     FBC_TRY(launch_warp<Prec>(P, uw, nw_max, st, launches));
+    FBC_CK(cudaEventRecord(g.evm, g.st));
     FBC_TRY(launch_block<Prec>(P, ub, nb_max, st, launches));
     FBC_CK(cudaEventRecord(g.ev1, g.st));
     int err = 0;
     FBC_CK(cudaMemcpyAsync(&err, (char*)g.ctr.p + 16, sizeof(int), cudaMemcpyDeviceToHost, g.st));
     FBC_CK(cudaStreamSynchronize(g.st));
     if (st) {
-        float ms = 0.f;
+        float ms = 0.f, mw = 0.f, mb = 0.f;
         FBC_CK(cudaEventElapsedTime(&ms, g.ev0, g.ev1));
+        FBC_CK(cudaEventElapsedTime(&mw, g.ev0, g.evm));
+        FBC_CK(cudaEventElapsedTime(&mb, g.evm, g.ev1));
         st->kernel_ms += ms;
+        st->warp_ms += uw.empty() ? 0.0 : mw;
+        st->block_ms += ub.empty() ? 0.0 : mb;
+        st->warp_units += (int64_t)uw.size();
+        st->block_units += (int64_t)ub.size();
+        for (const Unit& u : uw) st->warp_bytes += 40.0 * (double)P.seg_m[u.seg] + 52.0 * P.segs[u.seg].n;
+        for (const Unit& u : ub) st->block_bytes += 40.0 * (double)P.seg_m[u.seg] + 52.0 * P.segs[u.seg].n;
         st->units += (int64_t)P.units.size();
         double rel = 0;
         for (const Unit& u : P.units) rel += (double)P.seg_m[u.seg];
@@ -500,6 +509,7 @@ int fbc_gpu_init(int device) {
     FBC_CK(cudaStreamCreateWithFlags(&g.st, cudaStreamNonBlocking));
     FBC_CK(cudaEventCreate(&g.ev0));
     FBC_CK(cudaEventCreate(&g.ev1));
+    FBC_CK(cudaEventCreate(&g.evm));
     g.dev = device;
     g.init = true;
     return FBC_OK;
@@ -518,6 +528,7 @@ int fbc_gpu_shutdown(void) {
     g.wsw = Workspace();
     cudaEventDestroy(g.ev0);
     cudaEventDestroy(g.ev1);
+    cudaEventDestroy(g.evm);
     cudaStreamDestroy(g.st);
     g.init = false;
     return FBC_OK;

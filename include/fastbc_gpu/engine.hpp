@@ -1,0 +1,177 @@
+// C++ host layer over the C ABI of libfbcgpu (include/fbc_gpu.h).
+//
+// Header-only, no dependency on the reference headers: every engine is a template over a
+// graph type that offers the reference's IGraph surface (IGraph.h:30-58):
+//   vertices()        -> a sized container of vertex ids 0..n-1
+//   forwardStar(v)    -> a std::map<V, W> (destination -> weight), ascending destinations
+// and, for clusters, the ISubGraph surface (ISubGraph.h:13-40):
+//   vertices(), borders() -> std::set<V>, referenceGraph() -> shared_ptr<const IGraph>.
+// Errors from the C ABI are thrown as fbcgpu::Error (a std::runtime_error), the reference's
+// error style (std::invalid_argument / std::out_of_range are runtime exceptions too).
+#pragma once
+
+#include <cstdint>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <set>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../fbc_gpu.h"
+
+namespace fbcgpu {
+
+struct Error : std::runtime_error {
+    int code;
+    Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+inline void check(int rc) {
+    if (rc != FBC_OK) throw Error(rc, std::string("libfbcgpu: ") + fbc_last_error_string());
+}
+
+// Initialise the library on a device once per process.
+inline void ensure_device(int device = 0) {
+    static std::once_flag once;
+    static int rc = FBC_OK;
+    std::call_once(once, [&] { rc = fbc_gpu_init(device); });
+    check(rc);
+}
+
+// A device-resident copy of a graph (the GPU form of DirectedWeightedGraph).
+class DeviceGraph {
+  public:
+    DeviceGraph() = default;
+    DeviceGraph(const DeviceGraph&) = delete;
+    DeviceGraph& operator=(const DeviceGraph&) = delete;
+    ~DeviceGraph() {
+        if (h_) fbc_graph_free(h_);
+    }
+
+    // From any IGraph-like object: CSR rows are the forward stars in vertex-id order.
+    template <class G>
+    static std::shared_ptr<DeviceGraph> from_graph(const G& g, int device = 0) {
+        ensure_device(device);
+        const int64_t n = (int64_t)g.vertices().size();
+        std::vector<int64_t> rp((size_t)n + 1, 0);
+        std::vector<int32_t> col;
+        std::vector<double> w;
+        for (int64_t v = 0; v < n; ++v) {
+            for (const auto& e : g.forwardStar((typename std::decay<decltype(g.vertices()[0])>::type)v)) {
+                col.push_back((int32_t)e.first);
+                w.push_back((double)e.second);
+            }
+            rp[(size_t)v + 1] = (int64_t)col.size();
+        }
+        auto d = std::make_shared<DeviceGraph>();
+        check(fbc_graph_upload((int32_t)n, rp.data(), col.data(), w.data(), &d->h_));
+        d->n_ = (int32_t)n;
+        d->m_ = rp[(size_t)n];
+        return d;
+    }
+
+    fbc_graph handle() const { return h_; }
+    int32_t n() const { return n_; }
+    int64_t m() const { return m_; }
+
+  private:
+    fbc_graph h_ = nullptr;
+    int32_t n_ = 0;
+    int64_t m_ = 0;
+};
+
+// Caches the device copy of the last graph object it saw (the clustered pipeline calls
+// the single-source engine many times with the same graph).
+class GraphCache {
+  public:
+    template <class G>
+    std::shared_ptr<DeviceGraph> get(const std::shared_ptr<const G>& g, int device) {
+        std::lock_guard<std::mutex> lk(mu_);
+        if (!dev_ || key_ != (const void*)g.get()) {
+            dev_ = DeviceGraph::from_graph(*g, device);
+            key_ = (const void*)g.get();
+        }
+        return dev_;
+    }
+
+  private:
+    std::mutex mu_;
+    const void* key_ = nullptr;
+    std::shared_ptr<DeviceGraph> dev_;
+};
+
+struct Options {
+    int precision = FBC_PREC_FP64;
+    int sched = FBC_SCHED_BATCHED;
+    int device = 0;
+};
+
+// ExactBrandesBC::computeBC (ExactBrandesBC.h:45-95): BC over every source.
+template <class W, class G>
+std::vector<W> exact_bc(const G& g, const Options& o = {}) {
+    auto d = DeviceGraph::from_graph(g, o.device);
+    std::vector<double> bc((size_t)d->n());
+    check(fbc_exact_bc(d->handle(), o.precision, o.sched, bc.data(), nullptr));
+    return std::vector<W>(bc.begin(), bc.end());
+}
+
+// DijkstraSSBrandesBC::singleSourceBrandes (DijkstraSSBrandesBC.h:45-81).
+template <class W>
+std::vector<W> single_source(const DeviceGraph& d, int32_t source, const Options& o = {}) {
+    std::vector<double> dep((size_t)d.n());
+    check(fbc_single_source(d.handle(), source, o.precision, dep.data(), nullptr));
+    return std::vector<W>(dep.begin(), dep.end());
+}
+
+// Result of one cluster evaluation: intra BC per cluster vertex (cluster order) and the
+// (length, count) pair of each vertex to each border (DijkstraClusterEvaluator.h:166-177).
+struct ClusterResult {
+    std::vector<int32_t> vertices;
+    std::vector<int32_t> borders;        // ascending ids
+    std::vector<double> intra_bc;        // global ids (size n of the full graph)
+    std::vector<double> border_length;   // vertices.size() x borders.size()
+    std::vector<uint64_t> border_count;
+};
+
+// DijkstraClusterEvaluator::evaluateCluster over several clusters in one call.
+inline std::vector<double> cluster_eval_batch(const DeviceGraph& d,
+                                              const std::vector<std::vector<int32_t>>& clusters,
+                                              const std::vector<std::vector<int32_t>>& borders,
+                                              const Options& o, std::vector<double>* border_length,
+                                              std::vector<uint64_t>* border_count,
+                                              std::vector<int64_t>* entry_off) {
+    const int32_t nc = (int32_t)clusters.size();
+    std::vector<int64_t> coff((size_t)nc + 1, 0), boff((size_t)nc + 1, 0);
+    std::vector<int32_t> cv, bl;
+    if (entry_off) entry_off->assign((size_t)nc + 1, 0);
+    for (int32_t c = 0; c < nc; ++c) {
+        cv.insert(cv.end(), clusters[c].begin(), clusters[c].end());
+        bl.insert(bl.end(), borders[c].begin(), borders[c].end());
+        coff[c + 1] = (int64_t)cv.size();
+        boff[c + 1] = (int64_t)bl.size();
+        if (entry_off)
+            (*entry_off)[c + 1] = (*entry_off)[c] + (int64_t)clusters[c].size() * (int64_t)borders[c].size();
+    }
+    int64_t nb = 0, ent = 0;
+    check(fbc_cluster_border_count(d.handle(), nc, coff.data(), cv.data(), boff.data(), &nb, &ent));
+    std::vector<double> bc((size_t)d.n(), 0.0);
+    if (border_length) border_length->assign((size_t)ent, 0.0);
+    if (border_count) border_count->assign((size_t)ent, 0);
+    check(fbc_cluster_eval_batch(d.handle(), nc, coff.data(), cv.data(), boff.data(),
+                                 bl.empty() ? nullptr : bl.data(), o.precision, o.sched, bc.data(),
+                                 border_length ? border_length->data() : nullptr,
+                                 border_count ? border_count->data() : nullptr, nullptr));
+    return bc;
+}
+
+// The pivot loop of ClusteredBrandesBC.h:141-155 in one call: acc[v] += sum_p card_p * dep_p[v].
+inline void dependency_batch(const DeviceGraph& d, const std::vector<int32_t>& pivots,
+                             const std::vector<double>& cards, const Options& o,
+                             std::vector<double>& acc) {
+    check(fbc_sssp_dependency_batch(d.handle(), (int64_t)pivots.size(), pivots.data(), cards.data(),
+                                    o.precision, o.sched, acc.data(), nullptr));
+}
+
+}  // namespace fbcgpu

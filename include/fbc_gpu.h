@@ -61,6 +61,13 @@ typedef struct {
     double relaxations;      /* sum over units of the segment's edge count (TEPS numerator) */
     int32_t launches;        /* kernels launched by the call                               */
     int32_t slots;           /* concurrent block slots of the block-per-source kernel      */
+    double warp_ms;          /* device time of the warp-per-source kernel (CUDA events)    */
+    double block_ms;         /* device time of the block-per-source kernel (CUDA events)   */
+    double warp_bytes;       /* algorithmic bytes of the warp kernel's units               */
+    double block_bytes;      /* algorithmic bytes of the block kernel's units; one unit on a
+                                segment of n vertices and m edges counts 40*m + 52*n bytes  */
+    int64_t warp_units;
+    int64_t block_units;
 } fbc_stats;
 
 /* Library lifetime.  fbc_gpu_init selects the device and creates the library stream. */

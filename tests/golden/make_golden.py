@@ -1,0 +1,93 @@
+"""Regenerate the golden fixtures of tests/golden from the reference itself.
+
+Runs the reference fast-bc headers (compiled in place by ``make -C oracle ref`` into
+oracle/_ref/ref_harness) single-threaded on the seeded workloads and stores:
+  grid32_exact_bc.txt        ExactBrandesBC<int,double> over the 32x32 grid (%.17g)
+  grid32_ss.npz              DijkstraSSBrandesBC dependency vectors for a few sources
+  grid256_clustered.npz      the clustered run on the 256x256 grid (Louvain seeds 1-4,
+                             precision 0.01, kfrac 0.5): partition, borders, pivots and
+                             cardinalities, intra-cluster BC, final BC (step replay and the
+                             reference's own ClusteredBrandeBC::computeBC)
+  DWGtext.txt                the reference unit tests' 9-vertex fixture (copied)
+The clustered run takes about 15 minutes on one core.  Usage:
+  python tests/golden/make_golden.py [--reuse DIR]   (DIR: outputs of an earlier harness run)
+"""
+from __future__ import annotations
+
+import argparse
+import os
+import shutil
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+REF = "/root/reference"
+HARNESS = os.path.join(ROOT, "oracle", "_ref", "ref_harness")
+sys.path.insert(0, os.path.join(ROOT, "fast-bc_gb300"))
+import graphs  # noqa: E402
+
+ENV = dict(os.environ, OMP_NUM_THREADS="1")
+
+
+def run(*args, cwd=None):
+    subprocess.run([HARNESS, *map(str, args)], check=True, env=ENV, cwd=cwd)
+
+
+def parse_clusters(path):
+    with open(path) as f:
+        lines = f.read().split("\n")
+    nc = int(lines[0])
+    cv, bv, pv, kv = [], [], [], []
+    for c in range(nc):
+        rows = [list(map(int, lines[1 + 4 * c + k].split())) for k in range(4)]
+        for dst, r in zip((cv, bv, pv, kv), rows):
+            assert r[0] == len(r) - 1
+            dst.append(np.array(r[1:], np.int32))
+    def flat(lst):
+        off = np.zeros(len(lst) + 1, np.int64)
+        off[1:] = np.cumsum([x.size for x in lst])
+        return off, (np.concatenate(lst) if lst else np.zeros(0, np.int32)).astype(np.int32)
+    return flat(cv), flat(bv), flat(pv), flat(kv)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--reuse", default=None)
+    a = ap.parse_args()
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref", f"REF={REF}"], check=True)
+    shutil.copy(os.path.join(REF, "libfastbc", "test", "DWGtext.txt"), os.path.join(HERE, "DWGtext.txt"))
+    work = a.reuse or tempfile.mkdtemp()
+    g32 = os.path.join(work, "grid32.txt")
+    g256 = os.path.join(work, "grid256.txt")
+    if not os.path.exists(g32):
+        graphs.WORKLOADS["grid32"]().write(g32)
+    if not os.path.exists(g256):
+        graphs.WORKLOADS["grid256"]().write(g256)
+    run("exact", g32, os.path.join(HERE, "grid32_exact_bc.txt"))
+    srcs = [0, 77, 512, 1023]
+    deps = []
+    for s in srcs:
+        out = os.path.join(work, f"ss{s}.txt")
+        run("ss", g32, s, out)
+        deps.append(np.loadtxt(out))
+    np.savez_compressed(os.path.join(HERE, "grid32_ss.npz"), sources=np.array(srcs), dep=np.array(deps))
+    pre = os.path.join(work, "grid256")
+    if not os.path.exists(pre + ".bc_ref"):
+        run("clustered", g256, "1,2,3,4", 0.01, 0.5, pre)
+    (coff, cv), (boff, bv), (poff, pv), (koff, kv) = parse_clusters(pre + ".clusters")
+    assert np.array_equal(poff, koff)
+    bc = np.loadtxt(pre + ".bc")
+    bc_ref = np.loadtxt(pre + ".bc_ref")
+    assert np.array_equal(bc, bc_ref), "step replay differs from ClusteredBrandeBC::computeBC"
+    np.savez_compressed(os.path.join(HERE, "grid256_clustered.npz"), cluster_off=coff,
+                        cluster_vertices=cv, border_off=boff, borders=bv, pivot_off=poff,
+                        pivots=pv, cards=kv, intra_bc=np.loadtxt(pre + ".intra"), bc=bc)
+    print("golden fixtures written to", HERE)
+
+
+if __name__ == "__main__":
+    main()
