@@ -21,10 +21,9 @@
 //                  deterministic sum; then BC[v] += card * delta_v (ExactBrandesBC.h:86-89,
 //                  ClusteredBrandesBC.h:151-155).
 //
-// Two schedules share this code through the Group template:
-//   BlockGroup  one source per thread block, per-source state in a global-memory slot
-//   WarpGroup   one source per warp, per-source state in shared memory (small segments)
-// and two precision forms through the Prec template:
+// The block-per-source kernel below (per-source state in a global-memory slot) is the plain
+// schedule; batched_kernels.cuh holds the batched one.  Two precision forms share the code
+// through the Prec template:
 //   PrecF64     FP64 dependency arithmetic (the plain form)
 //   PrecDF32    FP32 double-float (two-sum compensated) dependency arithmetic; FP64 only
 //               for sigma ratios whose operands exceed 2^24 and for the BC reduction.
@@ -77,6 +76,9 @@ struct KParams {
     int64_t ws_stride;
     int32_t ws_n;                // capacity (vertices) of one slot / one shared-memory state
     int32_t iter_mult;           // distance-pass round cap = iter_mult * (n + 2)
+    int* retry_count;            // units to recompute on the plain kernel (batched only)
+    int* retry;
+    int32_t retry_cap;
     int32_t* dbg_dist;           // debug dump of one unit (may be null)
     unsigned long long* dbg_sig;
     double* dbg_dlt;
@@ -90,16 +92,6 @@ struct BlockGroup {
     __device__ static void sync() { __syncthreads(); }
     __device__ static int warp() { return threadIdx.x >> 5; }
     __device__ static int nwarps() { return blockDim.x >> 5; }
-};
-
-template <bool kSh>
-struct WarpGroup {
-    static constexpr bool kShared = kSh;
-    __device__ static int rank() { return threadIdx.x & 31; }
-    __device__ static int size() { return 32; }
-    __device__ static void sync() { __syncwarp(); }
-    __device__ static int warp() { return 0; }
-    __device__ static int nwarps() { return 1; }
 };
 
 // Loads of state that other threads modify with atomics: from L2 for global slots,
@@ -124,6 +116,8 @@ struct PrecF64 {
     __device__ static void add(Acc& a, unsigned long long sv, unsigned long long sw, D dw) {
         a.s += (double)sv / (double)sw * (1.0 + dw);
     }
+    // sigma_v == sigma_w: the ratio is exactly 1.0 and 1.0 * y == y
+    __device__ static void add_same(Acc& a, D dw) { a.s += 1.0 + dw; }
     __device__ static D store(const Acc& a) { return a.s; }
     __device__ static Acc load(D d) { return {d}; }
     __device__ static double value(const Acc& a) { return a.s; }
@@ -170,6 +164,16 @@ struct PrecDF32 {
         // acc += c
         two_sum(a.hi, ch, s, e);
         e = __fadd_rn(e, __fadd_rn(a.lo, cl));
+        fast_two_sum(s, e, a.hi, a.lo);
+    }
+    // sigma_v == sigma_w: r = (1, 0), so c = t exactly (the general path gives the same bits)
+    __device__ static void add_same(Acc& a, D dw) {
+        float s, e, th, tl;
+        two_sum(1.0f, dw.x, s, e);
+        e = __fadd_rn(e, dw.y);
+        fast_two_sum(s, e, th, tl);
+        two_sum(a.hi, th, s, e);
+        e = __fadd_rn(e, __fadd_rn(a.lo, tl));
         fast_two_sum(s, e, a.hi, a.lo);
     }
     __device__ static D store(const Acc& a) { return make_float2(a.hi, a.lo); }
@@ -563,43 +567,6 @@ __global__ void __launch_bounds__(1024) brandes_block_kernel(KParams P) {
         run_unit<BlockGroup, Prec>(P, u, S, C, epoch, P.ws_n);
     }
     if (threadIdx.x == 0) hdr[0] = epoch;
-}
-
-// Warp per source.  kSh: state in shared memory (P.ws_n vertices per warp, dynamic shared
-// memory of blockDim/32 states); otherwise one global-memory slot per warp.
-template <class Prec, bool kSh>
-__global__ void __launch_bounds__(256) brandes_warp_kernel(KParams P) {
-    extern __shared__ __align__(256) char smem[];
-    __shared__ Ctl Cs[8];
-    const int w = threadIdx.x >> 5;
-    const int64_t per = state_bytes<Prec>(P.ws_n);
-    Ctl& C = Cs[w];
-    unsigned epoch;
-    unsigned* hdr = nullptr;
-    State<Prec> S;
-    if constexpr (kSh) {
-        S = state_carve<Prec>(smem + (int64_t)w * per, P.ws_n);
-        state_init<WarpGroup<kSh>, Prec>(S, P.ws_n);
-        epoch = 1u;
-    } else {
-        char* slot = P.ws + ((int64_t)blockIdx.x * (blockDim.x >> 5) + w) * P.ws_stride;
-        hdr = (unsigned*)slot;
-        S = state_carve<Prec>(slot + 256, P.ws_n);
-        epoch = hdr[0];
-        if (epoch == 0u) {
-            state_init<WarpGroup<kSh>, Prec>(S, P.ws_n);
-            epoch = 1u;
-        }
-    }
-    for (;;) {
-        int ui = 0;
-        if ((threadIdx.x & 31) == 0) ui = (int)atomicAdd(P.next_unit, 1ull);
-        ui = __shfl_sync(kFull, ui, 0);
-        if (ui >= P.nunits) break;
-        const Unit u = P.units[ui];
-        run_unit<WarpGroup<kSh>, Prec>(P, u, S, C, epoch, P.ws_n);
-    }
-    if (!kSh && (threadIdx.x & 31) == 0) hdr[0] = epoch;
 }
 
 }  // namespace fbc

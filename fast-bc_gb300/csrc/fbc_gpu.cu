@@ -13,7 +13,7 @@
 #include <string>
 #include <vector>
 
-#include "brandes_kernels.cuh"
+#include "frontier_kernels.cuh"
 
 namespace {
 
@@ -76,11 +76,13 @@ struct DBuf {
 
 struct Options {
     int64_t delta = 0;          // bucket width; 0 = mean edge weight of the graph
-    int64_t block_threads = 256;
+    int64_t block_threads = 256;    // plain schedule
+    int64_t frontier_threads = 128; // batched schedule, large segments
     int64_t warp_max_n = 4096;  // batched: segments up to this size run one source per warp
     int64_t iter_mult = 16;
     int64_t ws_budget_mb = 0;   // 0 = 60% of the free device memory
     int64_t warp_smem = 1;      // batched: warp state in shared memory when it fits
+    int64_t debug_sched = FBC_SCHED_PLAIN;  // schedule used by fbc_sssp_debug
 };
 
 // A persistent workspace of equally sized slots.  Slot headers keep stamp counters, so a
@@ -101,7 +103,7 @@ struct Ctx {
     cudaStream_t st = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, evm = nullptr;
     Options opt;
-    DBuf segs, units_b, units_w, crp, cadj, cgid, cbord, bc, bdist, bsig, ctr, dbg;
+    DBuf retry, segs, units_b, units_w, chunks, crp, cadj, cgid, cbord, bc, bdist, bsig, ctr, dbg;
     Workspace wsb, wsw;
 };
 Ctx g;
@@ -118,6 +120,7 @@ struct fbc_graph_s {
     int32_t n = 0;
     int64_t m = 0;
     int32_t maxw = 0;
+    int32_t maxindeg = 0;
     double meanw = 1.0;
     int32_t* d_rp = nullptr;
     int2* d_adj = nullptr;
@@ -163,7 +166,10 @@ int make_graph(int32_t n, std::vector<int64_t>&& rp, std::vector<int32_t>&& col,
     }
     if ((double)n * (double)maxw > 2147483646.0)
         return fail(FBC_ERR_RANGE, "n * max_weight exceeds the int32 distance range");
+    std::vector<int32_t> indeg((size_t)std::max(n, 1), 0);
+    for (int64_t e = 0; e < m; ++e) indeg[col[e]]++;
     auto* G = new fbc_graph_s();
+    G->maxindeg = n ? *std::max_element(indeg.begin(), indeg.begin() + n) : 0;
     G->n = n;
     G->m = m;
     G->maxw = maxw;
@@ -207,6 +213,8 @@ int delta_for(double meanw) {
 struct Plan {
     std::vector<Seg> segs;
     std::vector<int64_t> seg_m;
+    std::vector<int32_t> seg_maxw;
+    std::vector<int32_t> seg_maxindeg;
     std::vector<Unit> units;
     int64_t bc_len = 0;
     int64_t border_entries = 0;
@@ -237,6 +245,9 @@ KParams base_params(const Plan& P) {
     K.bdist = g.bdist.as<double>();
     K.bsig = g.bsig.as<unsigned long long>();
     K.err = (int*)(g.ctr.as<unsigned long long>() + 2);
+    K.retry_count = K.err + 1;
+    K.retry = g.retry.as<int>();
+    K.retry_cap = (int32_t)(g.retry.cap / sizeof(int));
     K.iter_mult = (int32_t)g.opt.iter_mult;
     K.dbg_dist = P.dbg_dist;
     K.dbg_sig = P.dbg_sig;
@@ -265,19 +276,27 @@ int64_t ws_budget() {
     return b + (int64_t)g.wsb.buf.cap + (int64_t)g.wsw.buf.cap;
 }
 
+// Block-per-source launch with global-memory slots.  Plain schedule: brandes_block_kernel;
+// batched schedule: frontier_kernel.
 template <class Prec>
 int launch_block(const Plan& P, const std::vector<Unit>& units, int ws_n, fbc_stats* st,
-                 int& launches) {
+                 int& launches, bool force_plain = false) {
     if (units.empty()) return FBC_OK;
-    const int64_t stride = 256 + ((fbc::state_bytes<Prec>(ws_n) + 255) & ~int64_t(255));
-    int threads = (int)std::min<int64_t>(std::max<int64_t>(g.opt.block_threads, 32), 1024);
+    const bool fr = P.sched == FBC_SCHED_BATCHED && !force_plain;
+    const int64_t sb = fr ? fbc::fstate_bytes<Prec>(ws_n) : fbc::state_bytes<Prec>(ws_n);
+    const int64_t stride = 256 + ((sb + 255) & ~int64_t(255));
+    int threads = (int)std::min<int64_t>(std::max<int64_t>(fr ? g.opt.frontier_threads : g.opt.block_threads, 32),
+                                         fr ? 256 : 1024);
     threads = (threads / 32) * 32;
     int bps = 0;
-    FBC_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, fbc::brandes_block_kernel<Prec>, threads, 0));
+    if (fr) FBC_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, fbc::frontier_kernel<Prec>, threads, 0));
+    else FBC_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, fbc::brandes_block_kernel<Prec>, threads, 0));
     bps = std::max(bps, 1);
     int64_t slots = std::min<int64_t>((int64_t)g.nsm * bps, (int64_t)units.size());
     slots = std::max<int64_t>(1, std::min<int64_t>(slots, ws_budget() / stride));
-    FBC_TRY(ensure_ws(g.wsb, slots, stride, ws_n, (int)sizeof(typename Prec::D)));
+    // the two kernels keep different between-unit invariants: never share a workspace
+    Workspace& W = fr ? g.wsw : g.wsb;
+    FBC_TRY(ensure_ws(W, slots, stride, ws_n, (int)sizeof(typename Prec::D)));
     FBC_CK(g.units_b.ensure(sizeof(Unit) * units.size()));
     FBC_CK(cudaMemcpyAsync(g.units_b.p, units.data(), sizeof(Unit) * units.size(),
                            cudaMemcpyHostToDevice, g.st));
@@ -286,60 +305,70 @@ int launch_block(const Plan& P, const std::vector<Unit>& units, int ws_n, fbc_st
     K.units = g.units_b.as<Unit>();
     K.nunits = (int64_t)units.size();
     K.next_unit = g.ctr.as<unsigned long long>() + 0;
-    K.ws = g.wsb.buf.as<char>();
+    K.ws = W.buf.as<char>();
     K.ws_stride = stride;
     K.ws_n = ws_n;
-    fbc::brandes_block_kernel<Prec><<<(unsigned)slots, threads, 0, g.st>>>(K);
+    if (fr) fbc::frontier_kernel<Prec><<<(unsigned)slots, threads, 0, g.st>>>(K);
+    else fbc::brandes_block_kernel<Prec><<<(unsigned)slots, threads, 0, g.st>>>(K);
     FBC_CK(cudaGetLastError());
     ++launches;
     if (st) st->slots = (int32_t)slots;
     return FBC_OK;
 }
 
+// Batched schedule, small segments: (segment, chunk of sources) items, CSR and state in
+// shared memory.  `units` are grouped by segment.
+int64_t small_dyn_smem() { return (int64_t)g.smem_optin - 64; }
+
+bool small_fits(int nmax, int mmax, int warps) {
+    const fbc::SmallLayout L(nmax, mmax);
+    return L.pool + warps * fbc::SmallLayout::per_warp(nmax) <= small_dyn_smem();
+}
+
 template <class Prec>
-int launch_warp(const Plan& P, const std::vector<Unit>& units, int ws_n, fbc_stats* st,
-                int& launches) {
+int launch_small(const Plan& P, const std::vector<Unit>& units, int nmax, int mmax, int nmin,
+                 fbc_stats* st, int& launches) {
     if (units.empty()) return FBC_OK;
-    const int64_t per = fbc::state_bytes<Prec>(ws_n);
-    const int64_t avail = (int64_t)g.smem_optin - (int64_t)sizeof(fbc::Ctl) * 8 - 1024;
-    const int64_t wpb_fit = per > 0 ? avail / per : 0;
+    const fbc::SmallLayout L(nmax, mmax);
+    const int64_t dyn = small_dyn_smem();
+    if (!small_fits(nmax, mmax, 1)) return fail(FBC_ERR_INVALID_ARG, "small-segment kernel does not fit");
+    const int wpb = (int)std::max<int64_t>(
+        1, std::min<int64_t>(16, (dyn - L.pool) / fbc::SmallLayout::per_warp(std::max(nmin, 1))));
+    // chunks: consecutive units of one segment, enough of them to balance the SMs
+    std::vector<fbc::Chunk> ch;
+    const int64_t per_chunk = std::max<int64_t>(
+        2 * wpb, std::min<int64_t>(256, (int64_t)units.size() / std::max<int64_t>(1, (int64_t)g.nsm * 4)));
+    for (size_t i = 0; i < units.size();) {
+        size_t j = i;
+        while (j < units.size() && units[j].seg == units[i].seg && (int64_t)(j - i) < per_chunk) ++j;
+        ch.push_back(fbc::Chunk{units[i].seg, (int32_t)i, (int32_t)(j - i), 0});
+        i = j;
+    }
+    std::stable_sort(ch.begin(), ch.end(), [&](const fbc::Chunk& a, const fbc::Chunk& b) {
+        return P.segs[a.seg].n > P.segs[b.seg].n;
+    });
     FBC_CK(g.units_w.ensure(sizeof(Unit) * units.size()));
     FBC_CK(cudaMemcpyAsync(g.units_w.p, units.data(), sizeof(Unit) * units.size(),
                            cudaMemcpyHostToDevice, g.st));
-    if (st) st->h2d_bytes += (int64_t)(sizeof(Unit) * units.size());
-    KParams K = base_params(P);
-    K.units = g.units_w.as<Unit>();
-    K.nunits = (int64_t)units.size();
-    K.next_unit = g.ctr.as<unsigned long long>() + 1;
-    K.ws_n = ws_n;
-    if (g.opt.warp_smem && wpb_fit >= 1) {
-        const int wpb = (int)std::min<int64_t>(8, wpb_fit);
-        const size_t dyn = (size_t)(wpb * per);
-        auto kern = fbc::brandes_warp_kernel<Prec, true>;
-        FBC_CK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
-        int bps = 0;
-        FBC_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kern, 32 * wpb, dyn));
-        bps = std::max(bps, 1);
-        int64_t blocks = std::min<int64_t>((int64_t)g.nsm * bps,
-                                           ((int64_t)units.size() + wpb - 1) / wpb);
-        kern<<<(unsigned)blocks, 32 * wpb, dyn, g.st>>>(K);
-        FBC_CK(cudaGetLastError());
-    } else {
-        const int wpb = 8;
-        const int64_t stride = 256 + ((per + 255) & ~int64_t(255));
-        auto kern = fbc::brandes_warp_kernel<Prec, false>;
-        int bps = 0;
-        FBC_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kern, 32 * wpb, 0));
-        bps = std::max(bps, 1);
-        int64_t blocks = std::min<int64_t>((int64_t)g.nsm * bps,
-                                           ((int64_t)units.size() + wpb - 1) / wpb);
-        blocks = std::max<int64_t>(1, std::min<int64_t>(blocks, ws_budget() / (stride * wpb)));
-        FBC_TRY(ensure_ws(g.wsw, blocks * wpb, stride, ws_n, (int)sizeof(typename Prec::D)));
-        K.ws = g.wsw.buf.as<char>();
-        K.ws_stride = stride;
-        kern<<<(unsigned)blocks, 32 * wpb, 0, g.st>>>(K);
-        FBC_CK(cudaGetLastError());
-    }
+    FBC_CK(g.chunks.ensure(sizeof(fbc::Chunk) * ch.size()));
+    FBC_CK(cudaMemcpyAsync(g.chunks.p, ch.data(), sizeof(fbc::Chunk) * ch.size(),
+                           cudaMemcpyHostToDevice, g.st));
+    if (st) st->h2d_bytes += (int64_t)(sizeof(Unit) * units.size() + sizeof(fbc::Chunk) * ch.size());
+    fbc::SmallParams S{};
+    S.k = base_params(P);
+    S.k.units = g.units_w.as<Unit>();
+    S.k.nunits = (int64_t)units.size();
+    S.chunks = g.chunks.as<fbc::Chunk>();
+    S.nchunks = (int32_t)ch.size();
+    S.nmax = nmax;
+    S.mmax = mmax;
+    S.smem = (int32_t)dyn;
+    S.next_chunk = g.ctr.as<unsigned long long>() + 1;
+    auto kern = fbc::small_seg_kernel<Prec>;
+    FBC_CK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
+    const int64_t blocks = std::min<int64_t>((int64_t)g.nsm, (int64_t)ch.size());
+    kern<<<(unsigned)blocks, 32 * wpb, (size_t)dyn, g.st>>>(S);
+    FBC_CK(cudaGetLastError());
     ++launches;
     return FBC_OK;
 }
@@ -366,34 +395,77 @@ int run_plan_t(Plan& P, fbc_stats* st) {
     FBC_CK(cudaMemsetAsync(g.ctr.p, 0, 64, g.st));
     if (st) st->h2d_bytes += (int64_t)(sizeof(Seg) * P.segs.size());
 
-    // split units by schedule; biggest segments first (longest-processing-time order)
+    // split units by schedule.  Batched: segments that fit the shared-memory kernel run
+    // there (grouped by segment); the rest run block-per-source, biggest segments first.
     std::vector<Unit> ub, uw;
-    int nb_max = 0, nw_max = 0;
-    for (const Unit& u : P.units) {
-        const int n = P.segs[u.seg].n;
-        if (P.sched == FBC_SCHED_BATCHED && n <= g.opt.warp_max_n) {
-            uw.push_back(u);
-            nw_max = std::max(nw_max, n);
-        } else {
-            ub.push_back(u);
-            nb_max = std::max(nb_max, n);
+    int nb_max = 0, nw_max = 0, mw_max = 0;
+    std::vector<char> small(P.segs.size(), 0);
+    if (P.sched == FBC_SCHED_BATCHED && !P.dbg_dist) {  // debug dumps come from block kernels
+        for (size_t s = 0; s < P.segs.size(); ++s) {
+            const int n = P.segs[s].n;
+            small[s] = n <= std::min<int64_t>(g.opt.warp_max_n, 65535) && P.seg_maxw[s] < 65536 &&
+                       P.seg_m[s] < ((int64_t)1 << 30);
         }
     }
-    auto by_size = [&](const Unit& a, const Unit& b) {
+    // the shared-memory layout is sized by the largest small segment: demote the largest
+    // ones until at least two warps fit
+    for (;;) {
+        int nm = 0, mm = 0, arg = -1;
+        for (size_t s = 0; s < P.segs.size(); ++s)
+            if (small[s]) {
+                mm = std::max<int>(mm, (int)P.seg_m[s]);
+                if (P.segs[s].n >= nm) { nm = P.segs[s].n; arg = (int)s; }
+            }
+        if (arg < 0 || small_fits(nm, mm, 2)) break;
+        small[arg] = 0;
+    }
+    int nw_min = 1 << 30;
+    std::vector<std::vector<Unit>> by_seg(P.segs.size());
+    for (const Unit& u : P.units) {
+        if (small[u.seg]) {
+            by_seg[u.seg].push_back(u);
+            nw_max = std::max(nw_max, P.segs[u.seg].n);
+            nw_min = std::min(nw_min, P.segs[u.seg].n);
+            mw_max = std::max<int>(mw_max, (int)P.seg_m[u.seg]);
+        } else {
+            ub.push_back(u);
+            nb_max = std::max(nb_max, P.segs[u.seg].n);
+        }
+    }
+    for (auto& v : by_seg) uw.insert(uw.end(), v.begin(), v.end());
+    std::stable_sort(ub.begin(), ub.end(), [&](const Unit& a, const Unit& b) {
         return P.segs[a.seg].n > P.segs[b.seg].n;
-    };
-    std::stable_sort(uw.begin(), uw.end(), by_size);
-    std::stable_sort(ub.begin(), ub.end(), by_size);
-
+    });
+    // the batched block kernel keeps tight in-edge counts in 16 bits
+    if (P.sched == FBC_SCHED_BATCHED)
+        for (const Unit& u : ub)
+            if (P.seg_maxindeg[u.seg] >= 65535) {
+                P.sched = FBC_SCHED_PLAIN;
+                break;
+            }
     int launches = 0;
     FBC_CK(cudaEventRecord(g.ev0, g.st));
-    FBC_TRY(launch_warp<Prec>(P, uw, nw_max, st, launches));
+    FBC_CK(g.retry.ensure(sizeof(int) * std::max<size_t>(ub.size(), 1)));
+    FBC_TRY(launch_small<Prec>(P, uw, nw_max, mw_max, nw_min, st, launches));
     FBC_CK(cudaEventRecord(g.evm, g.st));
     FBC_TRY(launch_block<Prec>(P, ub, nb_max, st, launches));
-    FBC_CK(cudaEventRecord(g.ev1, g.st));
-    int err = 0;
-    FBC_CK(cudaMemcpyAsync(&err, (char*)g.ctr.p + 16, sizeof(int), cudaMemcpyDeviceToHost, g.st));
+    int err[2] = {0, 0};
+    FBC_CK(cudaMemcpyAsync(err, (char*)g.ctr.p + 16, 2 * sizeof(int), cudaMemcpyDeviceToHost, g.st));
     FBC_CK(cudaStreamSynchronize(g.st));
+    if (err[1] > 0 && err[0] == 0) {
+        // units whose path counts outgrew the batched kernel's 48-bit field: recompute them
+        // with the plain kernel (64-bit counts); nothing of theirs was accumulated yet
+        std::vector<int> idx((size_t)err[1]);
+        FBC_CK(cudaMemcpy(idx.data(), g.retry.p, sizeof(int) * idx.size(), cudaMemcpyDeviceToHost));
+        std::vector<Unit> again;
+        for (int i : idx) again.push_back(ub[(size_t)i]);
+        FBC_CK(cudaMemsetAsync(g.ctr.p, 0, 8, g.st));
+        FBC_TRY(launch_block<Prec>(P, again, nb_max, st, launches, true));
+        FBC_CK(cudaMemcpyAsync(err, (char*)g.ctr.p + 16, sizeof(int), cudaMemcpyDeviceToHost, g.st));
+    }
+    FBC_CK(cudaEventRecord(g.ev1, g.st));
+    FBC_CK(cudaStreamSynchronize(g.st));
+    int errv = err[0];
     if (st) {
         float ms = 0.f, mw = 0.f, mb = 0.f;
         FBC_CK(cudaEventElapsedTime(&ms, g.ev0, g.ev1));
@@ -412,7 +484,7 @@ int run_plan_t(Plan& P, fbc_stats* st) {
         st->relaxations += rel;
         st->launches += launches;
     }
-    return map_err(err);
+    return map_err(errv);
 }
 
 int run_plan(Plan& P, fbc_stats* st) {
@@ -519,7 +591,7 @@ int fbc_gpu_shutdown(void) {
     std::lock_guard<std::recursive_mutex> lk(g_mu);
     if (!g.init) return FBC_OK;
     cudaStreamSynchronize(g.st);
-    for (DBuf* b : {&g.segs, &g.units_b, &g.units_w, &g.crp, &g.cadj, &g.cgid, &g.cbord, &g.bc,
+    for (DBuf* b : {&g.retry, &g.segs, &g.units_b, &g.units_w, &g.chunks, &g.crp, &g.cadj, &g.cgid, &g.cbord, &g.bc,
                     &g.bdist, &g.bsig, &g.ctr, &g.dbg})
         b->release();
     g.wsb.buf.release();
@@ -540,10 +612,12 @@ int fbc_set_option(const char* key, int64_t value) {
     std::string k(key);
     if (k == "delta") g.opt.delta = std::max<int64_t>(0, value);
     else if (k == "block_threads") g.opt.block_threads = std::max<int64_t>(32, std::min<int64_t>(1024, value));
+    else if (k == "frontier_threads") g.opt.frontier_threads = std::max<int64_t>(32, std::min<int64_t>(256, value));
     else if (k == "warp_max_n") g.opt.warp_max_n = std::max<int64_t>(0, value);
     else if (k == "iter_mult") g.opt.iter_mult = std::max<int64_t>(1, std::min<int64_t>(1 << 20, value));
     else if (k == "ws_budget_mb") g.opt.ws_budget_mb = std::max<int64_t>(0, value);
     else if (k == "warp_smem") g.opt.warp_smem = value ? 1 : 0;
+    else if (k == "debug_sched") g.opt.debug_sched = value ? FBC_SCHED_BATCHED : FBC_SCHED_PLAIN;
     else return fail(FBC_ERR_INVALID_ARG, "unknown option " + k);
     return FBC_OK;
 }
@@ -554,10 +628,12 @@ int fbc_get_option(const char* key, int64_t* value) {
     std::string k(key);
     if (k == "delta") *value = g.opt.delta;
     else if (k == "block_threads") *value = g.opt.block_threads;
+    else if (k == "frontier_threads") *value = g.opt.frontier_threads;
     else if (k == "warp_max_n") *value = g.opt.warp_max_n;
     else if (k == "iter_mult") *value = g.opt.iter_mult;
     else if (k == "ws_budget_mb") *value = g.opt.ws_budget_mb;
     else if (k == "warp_smem") *value = g.opt.warp_smem;
+    else if (k == "debug_sched") *value = g.opt.debug_sched;
     else return fail(FBC_ERR_INVALID_ARG, "unknown option " + k);
     return FBC_OK;
 }
@@ -658,6 +734,8 @@ int fbc_exact_bc(fbc_graph G, int precision, int sched, double* out_bc, fbc_stat
     P.sched = sched;
     P.segs.push_back(whole_graph_seg(G, 0));
     P.seg_m.push_back(G->m);
+    P.seg_maxw.push_back(G->maxw);
+    P.seg_maxindeg.push_back(G->maxindeg);
     for (int32_t s = 0; s < G->n; ++s) P.units.push_back(Unit{0, s, 1.0, -1});
     P.bc_len = G->n;
     FBC_TRY(run_plan(P, st));
@@ -681,6 +759,8 @@ int fbc_sssp_dependency_batch(fbc_graph G, int64_t count, const int32_t* sources
     P.sched = sched;
     P.segs.push_back(whole_graph_seg(G, 0));
     P.seg_m.push_back(G->m);
+    P.seg_maxw.push_back(G->maxw);
+    P.seg_maxindeg.push_back(G->maxindeg);
     for (int64_t i = 0; i < count; ++i) {
         if (sources[i] < 0 || sources[i] >= G->n) return fail(FBC_ERR_INVALID_ARG, "source out of range");
         P.units.push_back(Unit{0, sources[i], cards ? cards[i] : 1.0, -1});
@@ -829,6 +909,8 @@ int fbc_cluster_eval_batch(fbc_graph G, int32_t nclusters, const int64_t* coff,
         s.delta = dl;
         P.segs.push_back(s);
         P.seg_m.push_back(seg_m[c]);
+        P.seg_maxw.push_back(G->maxw);
+    P.seg_maxindeg.push_back(G->maxindeg);
         for (int32_t i = 0; i < s.n; ++i) P.units.push_back(Unit{c, i, 1.0, ent + (int64_t)i * s.nb});
         ent += (int64_t)s.n * s.nb;
     }
@@ -864,6 +946,8 @@ int fbc_multi_exact_bc(int32_t ngraphs, const fbc_graph* graphs, int precision, 
         if (!graphs[i]) return fail(FBC_ERR_INVALID_ARG, "null graph in batch");
         P.segs.push_back(whole_graph_seg(graphs[i], base[i]));
         P.seg_m.push_back(graphs[i]->m);
+        P.seg_maxw.push_back(graphs[i]->maxw);
+        P.seg_maxindeg.push_back(graphs[i]->maxindeg);
         for (int32_t s = 0; s < graphs[i]->n; ++s) P.units.push_back(Unit{i, s, 1.0, -1});
         base[i + 1] = base[i] + graphs[i]->n;
     }
@@ -887,9 +971,11 @@ int fbc_sssp_debug(fbc_graph G, int32_t source, int32_t* out_dist, uint64_t* out
     char* base = g.dbg.as<char>();
     Plan P;
     P.prec = FBC_PREC_FP64;
-    P.sched = FBC_SCHED_PLAIN;
+    P.sched = (int)g.opt.debug_sched;
     P.segs.push_back(whole_graph_seg(G, 0));
     P.seg_m.push_back(G->m);
+    P.seg_maxw.push_back(G->maxw);
+    P.seg_maxindeg.push_back(G->maxindeg);
     P.units.push_back(Unit{0, source, 1.0, -1});
     P.bc_len = G->n;
     P.dbg_sig = (unsigned long long*)base;

@@ -82,10 +82,13 @@ def main():
     assert np.array_equal(poff, koff)
     bc = np.loadtxt(pre + ".bc")
     bc_ref = np.loadtxt(pre + ".bc_ref")
-    assert np.array_equal(bc, bc_ref), "step replay differs from ClusteredBrandeBC::computeBC"
+    # the replay adds straight into globalBC; computeBC's one-thread OpenMP reduction adds a
+    # private sum at the end, so the two agree to rounding only
+    assert np.max(np.abs(bc - bc_ref)) <= 1e-12 * np.max(np.abs(bc_ref)), "replay != computeBC"
     np.savez_compressed(os.path.join(HERE, "grid256_clustered.npz"), cluster_off=coff,
                         cluster_vertices=cv, border_off=boff, borders=bv, pivot_off=poff,
-                        pivots=pv, cards=kv, intra_bc=np.loadtxt(pre + ".intra"), bc=bc)
+                        pivots=pv, cards=kv, intra_bc=np.loadtxt(pre + ".intra"), bc=bc_ref,
+                        bc_replay=bc)
     print("golden fixtures written to", HERE)
 
 

@@ -205,3 +205,78 @@ def test_duplicate_edges_summed(fg):
     rp, col, w = g.csr()
     assert g.n == 3 and g.m == 4
     assert list(col[rp[0]:rp[1]]) == [1, 2] and list(w[rp[0]:rp[1]]) == [4.0, 5.0]
+
+
+def _clustered_inputs(fg):
+    import os
+    from conftest import GOLDEN
+
+    z = np.load(os.path.join(GOLDEN, "grid256_clustered.npz"))
+    off, cv, boff, bv = z["cluster_off"], z["cluster_vertices"], z["border_off"], z["borders"]
+    poff, pv, kv = z["pivot_off"], z["pivots"], z["cards"]
+    keep = [c for c in range(off.size - 1) if boff[c + 1] > boff[c]]
+    cs = fg.ClusterSet.from_lists([cv[off[c]:off[c + 1]] for c in keep],
+                                  [bv[boff[c]:boff[c + 1]] for c in keep])
+    piv = [pv[poff[c]:poff[c + 1]] for c in keep]
+    crd = [kv[poff[c]:poff[c + 1]] for c in keep]
+    return z, keep, cs, piv, crd
+
+
+@pytest.mark.parametrize("prec,sched", [(0, 0), (0, 1), (1, 1)])
+def test_grid256_clustered_matches_reference(fg, prec, sched):
+    """The full clustered pipeline (reference partition + pivots) against the reference's own
+    ClusteredBrandeBC::computeBC output.  The result is a cancellation (intra + sum dep*card -
+    sum intra*card, most entries negative), so the bound is |err| / max|BC|; intra BC is
+    checked elementwise."""
+    z, keep, cs, piv, crd = _clustered_inputs(fg)
+    el = graphs.WORKLOADS["grid256"]()
+    g = fg.Graph.from_edgelist(el)
+    tol = TOL_FP64 if prec == 0 else TOL_FP32C
+    ev = fg.cluster_eval_batch(g, cs, prec, sched)
+    assert rel_err(ev.intra_bc, z["intra_bc"]) <= tol
+    bc = fg.clustered_bc(g, cs, piv, crd, prec, sched, ev=ev)
+    golden = z["bc"]
+    assert np.max(np.abs(bc - golden)) / np.max(np.abs(golden)) <= tol
+
+
+def test_grid256_cluster_border_vectors(fg):
+    """VertexInfo (border length, count) of three reference clusters: bit-exact."""
+    z, keep, cs, piv, crd = _clustered_inputs(fg)
+    el = graphs.WORKLOADS["grid256"]()
+    og = oracle.CSR.from_edgelist(el)
+    g = fg.Graph.from_edgelist(el)
+    ev = fg.cluster_eval_batch(g, cs, fg.FP32C, fg.BATCHED)
+    for c in (0, 11, len(keep) - 1):
+        vs = cs.vertices[cs.off[c]:cs.off[c + 1]]
+        b = cs.borders[cs.boff[c]:cs.boff[c + 1]]
+        _, bd, bs = oracle.cluster_eval(og, vs, b)
+        for i in range(vs.size):
+            L, Cn = ev.vertex_info(c, i)
+            assert np.array_equal(L, bd[i]) and np.array_equal(Cn.astype(np.float64), bs[i])
+
+
+@pytest.mark.parametrize("sched", [0, 1])
+def test_grid256_sources_bit_exact_both_schedules(fg, sched):
+    """Distances, path counts and predecessor counts from the plain block kernel and from the
+    batched frontier kernel (64-bit (dist|stamp) words, packed sigma|counter)."""
+    el = graphs.WORKLOADS["grid256"]()
+    og = oracle.CSR.from_edgelist(el)
+    g = fg.Graph.from_edgelist(el)
+    fg.set_option("debug_sched", sched)
+    try:
+        for src in (3, 40000):
+            check_source(fg, g, og, src)
+    finally:
+        fg.set_option("debug_sched", 0)
+
+
+def test_rgg_sources_bit_exact_batched(fg):
+    el = graphs.rgg_knn(20000, seed=13)
+    og = oracle.CSR.from_edgelist(el)
+    g = fg.Graph.from_edgelist(el)
+    fg.set_option("debug_sched", 1)
+    try:
+        for src in (0, 19999):
+            check_source(fg, g, og, src)
+    finally:
+        fg.set_option("debug_sched", 0)

@@ -79,3 +79,31 @@ def test_single_source_and_dump_consistent():
     assert order[0] == 77 and np.all(np.diff(dist[order]) >= 0)
     for v in range(g.n):
         assert sig[v] == sum(sig[p] for p in preds[v]) or v == 77
+
+
+def test_grid32_single_source_matches_reference():
+    z = np.load(os.path.join(GOLDEN, "grid32_ss.npz"))
+    g = oracle.CSR.from_edgelist(graphs.WORKLOADS["grid32"]())
+    for s, dep in zip(z["sources"], z["dep"]):
+        assert np.array_equal(oracle.single_source(g, int(s)), dep)
+
+
+def test_grid256_clusters_match_reference_intra_bc():
+    """DijkstraClusterEvaluator on the reference's own Louvain clusters: bit-identical."""
+    z = np.load(os.path.join(GOLDEN, "grid256_clustered.npz"))
+    g = oracle.CSR.from_edgelist(graphs.WORKLOADS["grid256"]())
+    off, cv, boff, bv = z["cluster_off"], z["cluster_vertices"], z["border_off"], z["borders"]
+    acc = np.zeros(g.n)
+    for c in (0, 7, 33):
+        vs = cv[off[c]:off[c + 1]]
+        oracle.cluster_eval(g, vs, bv[boff[c]:boff[c + 1]], acc)
+        assert np.array_equal(acc[vs], z["intra_bc"][vs])
+
+
+def test_generators_are_stable():
+    """The seeded generators are part of the workload definition."""
+    el = graphs.WORKLOADS["grid256"]()
+    assert (el.n, el.m) == (65536, 248528)
+    assert int(el.w.sum()) == 12506652
+    assert graphs.WORKLOADS["grid32"]().m == 3968
+    assert graphs.rgg_sizes()[:3] == [1765, 2433, 1422]
