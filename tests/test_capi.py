@@ -1,0 +1,39 @@
+"""The C ABI library loads and exports every entry point include/fbc_gpu.h declares (CPU only:
+no compute call is made; without a GPU fbc_gpu_init reports a CUDA error)."""
+import ctypes as C
+import os
+import re
+
+from conftest import ROOT
+
+HEADER = os.path.join(ROOT, "include", "fbc_gpu.h")
+LIB = os.path.join(ROOT, "fast-bc_gb300", "libfbcgpu.so")
+
+
+def declared():
+    src = open(HEADER).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(fbc_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_header_declares_the_boundary():
+    names = declared()
+    for must in ("fbc_gpu_init", "fbc_exact_bc", "fbc_single_source", "fbc_sssp_dependency_batch",
+                 "fbc_cluster_eval_batch", "fbc_multi_exact_bc", "fbc_sssp_debug", "fbc_last_error_string"):
+        assert must in names
+
+
+def test_library_exports_every_declared_symbol():
+    lib = C.CDLL(LIB)
+    missing = [n for n in declared() if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_calls_fail_cleanly_before_init():
+    lib = C.CDLL(LIB)
+    lib.fbc_last_error_string.restype = C.c_char_p
+    out = C.c_void_p()
+    rp = (C.c_int64 * 2)(0, 0)
+    rc = lib.fbc_graph_upload(1, rp, None, None, C.byref(out))
+    assert rc in (7, 2)  # FBC_ERR_NOT_INIT (or a CUDA error where no driver is present)
+    assert lib.fbc_last_error_string()
