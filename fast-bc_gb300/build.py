@@ -12,8 +12,10 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = [os.path.join(HERE, "csrc", "fbc_gpu.cu")]
-HEADERS = [os.path.join(HERE, "csrc", "brandes_kernels.cuh"), os.path.join(ROOT, "include", "fbc_gpu.h")]
+SOURCES = [os.path.join(HERE, "csrc", "fbc_gpu.cu"), os.path.join(HERE, "csrc", "noalloc.cu")]
+HEADERS = [os.path.join(HERE, "csrc", f) for f in
+           ("brandes_kernels.cuh", "batched_kernels.cuh", "frontier_kernels.cuh")] + \
+          [os.path.join(ROOT, "include", "fbc_gpu.h")]
 OUT = os.path.join(HERE, "libfbcgpu.so")
 
 

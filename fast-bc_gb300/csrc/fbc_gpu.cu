@@ -561,6 +561,9 @@ int cluster_ids(const fbc_graph_s* G, int32_t nclusters, const int64_t* coff, co
 
 }  // namespace
 
+// Error text of the calling thread, shared with the other translation units of the library.
+void fbc_internal_set_error(const char* msg) { g_err = msg ? msg : ""; }
+
 // ============================================================================ C ABI
 extern "C" {
 
