@@ -151,6 +151,255 @@ def cpu_sample(el, z, threads: int, budget_s: float = 12.0):
     return work / dt / 1e9, dt, f"{done_c} of {len(keep)} clusters + {done_p} of {pv.size} pivots"
 
 
+class Workload:
+    """A configuration measured by --workload (default: the clustered 256x256 grid)."""
+
+    name = ""
+    config: dict = {}
+    work = 0.0
+
+    def setup(self, fg, args):
+        raise NotImplementedError
+
+    def step(self, fg, prec, sched):
+        """Run one step; returns the list of fbc Stats of its C-ABI calls."""
+        raise NotImplementedError
+
+    def cpu_sample(self, threads, budget_s):
+        raise NotImplementedError
+
+
+def _tile_partition(rows, cols, tile):
+    ids = np.arange(rows * cols, dtype=np.int64)
+    t = (ids // cols) // tile * ((cols + tile - 1) // tile) + (ids % cols) // tile
+    order = np.argsort(t, kind="stable")
+    counts = np.bincount(t)
+    off = np.zeros(counts.size + 1, np.int64)
+    off[1:] = np.cumsum(counts)
+    return off, order.astype(np.int32)
+
+
+def _pivots_for(off, cv, frac, seed):
+    """Synthetic pivot classes: about `frac` of each cluster's vertices, cardinalities summing to
+    the cluster size (the reference's pivot density on the 256x256 grid is ~3.9%)."""
+    import graphs
+
+    piv, cards = [], []
+    for c in range(off.size - 1):
+        vs = cv[off[c]:off[c + 1]]
+        k = max(1, int(round(frac * vs.size)))
+        key = graphs.rand_u64(seed, 300 + c, np.arange(vs.size))
+        pick = np.argsort(key)[:k]
+        p = np.sort(vs[pick]).astype(np.int32)
+        base = np.full(k, vs.size // k, np.int64)
+        base[: vs.size - base.sum()] += 1
+        piv.append(p)
+        cards.append(base.astype(np.float64))
+    return piv, cards
+
+
+class GridClustered4M(Workload):
+    """The full form: 2048x2048 road grid (4,194,304 vertices), highway p=0.1%, radius 128.
+    Stand-ins, because the reference cannot produce them at this size (its clustered run takes
+    days): square tiles of 121x121 for the Louvain partition and a seeded 3.9% pivot set per
+    tile.  --fraction samples whole tiles and pivots so that a step fits a bench run."""
+
+    name = "grid2048-clustered"
+
+    def setup(self, fg, args):
+        import graphs
+
+        el = graphs.WORKLOADS["grid2048"]()
+        self.el = el
+        off, cv = _tile_partition(2048, 2048, 121)
+        piv, cards = _pivots_for(off, cv, 0.039, 11)
+        nt = off.size - 1
+        step = max(1, int(round(1.0 / args.fraction)))
+        self.keep = list(range(0, nt, step))
+        self.clusters = [cv[off[c]:off[c + 1]] for c in self.keep]
+        self.g = fg.Graph.from_edgelist(el)
+        self.cs = fg.ClusterSet.from_lists(self.clusters).with_borders(self.g)
+        allp = np.concatenate(piv)
+        allc = np.concatenate(cards)
+        sel = np.arange(0, allp.size, step)
+        self.pv, self.kv = allp[sel], allc[sel]
+        rp, col, _ = el.csr()
+        cid = np.full(el.n, -1, np.int64)
+        for k, c in enumerate(self.keep):
+            cid[cv[off[c]:off[c + 1]]] = k
+        src = np.repeat(np.arange(el.n), np.diff(rp))
+        intra = (cid[src] >= 0) & (cid[src] == cid[col])
+        mc = np.bincount(cid[src][intra], minlength=len(self.keep))
+        self.work = float(sum(len(self.clusters[k]) * mc[k] for k in range(len(self.keep))) + self.pv.size * el.m)
+        self.config = {"workload": "clustered fast-bc, 2048x2048 road grid (4,194,304 vertices, "
+                                   f"{el.m:,} edges)", "graph_seed": 42,
+                       "partition": "121x121 tiles standing in for Louvain", "pivots": "seeded 3.9% per tile",
+                       "sample": f"{len(self.keep)} of {nt} tiles and {self.pv.size} of {allp.size} pivots",
+                       "relaxations_per_step": self.work}
+
+    def step(self, fg, prec, sched):
+        st1, st2 = fg.Stats(), fg.Stats()
+        ev = fg.cluster_eval_batch(self.g, self.cs, prec, sched, stats=st1)
+        fg.dependency_batch(self.g, self.pv, self.kv, prec, sched, out=ev.intra_bc.copy(), stats=st2)
+        return [st1, st2]
+
+    def cpu_sample(self, threads, budget_s):
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle
+
+        og = oracle.CSR.from_edgelist(self.el)
+        t0 = time.perf_counter()
+        k = max(threads, 1)
+        oracle.pivot_batch(og, self.pv[:k], self.kv[:k], threads=threads)
+        dt = time.perf_counter() - t0
+        return k * self.el.m / dt / 1e9, dt, f"{k} pivot SSSPs on the 4M-vertex graph"
+
+
+class ExactWorkload(Workload):
+    """Exact Brandes over every source of one graph (the precision configuration: 512x512 grid)."""
+
+    def __init__(self, name, key):
+        self.name, self.key = name, key
+
+    def setup(self, fg, args):
+        import graphs
+
+        self.el = graphs.WORKLOADS[self.key]()
+        self.g = fg.Graph.from_edgelist(self.el)
+        self.work = float(self.el.n) * self.el.m
+        self.config = {"workload": f"exact Brandes, {self.key} road grid ({self.el.n:,} vertices, "
+                                   f"{self.el.m:,} edges), every source", "graph_seed": 42,
+                       "relaxations_per_step": self.work}
+
+    def step(self, fg, prec, sched):
+        st = fg.Stats()
+        self.last = fg.exact_bc(self.g, prec, sched, stats=st)
+        return [st]
+
+    def cpu_sample(self, threads, budget_s):
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle
+
+        og = oracle.CSR.from_edgelist(self.el)
+        k = max(threads, 1) * 4
+        src = np.arange(0, self.el.n, max(1, self.el.n // k))[:k].astype(np.int32)
+        t0 = time.perf_counter()
+        oracle.exact_bc_sources(og, src, threads=threads)
+        dt = time.perf_counter() - t0
+        return src.size * self.el.m / dt / 1e9, dt, f"{src.size} of {self.el.n} sources"
+
+
+class MultiGraph(Workload):
+    """Batching: 48 random geometric 3-NN graphs, exact Brandes on each, one persistent launch
+    (--sequential: 48 separate calls instead)."""
+
+    name = "rgg48-exact"
+
+    def setup(self, fg, args):
+        import graphs
+
+        self.els = graphs.rgg_batch(48)
+        self.gs = [fg.Graph.from_edgelist(e) for e in self.els]
+        self.sequential = args.sequential
+        self.work = float(sum(e.n * e.m for e in self.els))
+        self.config = {"workload": "48 random geometric 3-NN graphs, n log-uniform in [1024, 65536], exact "
+                                   "Brandes on each", "graph_seed": 7, "sequential": bool(args.sequential),
+                       "relaxations_per_step": self.work}
+
+    def step(self, fg, prec, sched):
+        if self.sequential:
+            out = []
+            for g in self.gs:
+                st = fg.Stats()
+                fg.exact_bc(g, prec, sched, stats=st)
+                out.append(st)
+            return out
+        st = fg.Stats()
+        fg.multi_exact_bc(self.gs, prec, sched, stats=st)
+        return [st]
+
+    def cpu_sample(self, threads, budget_s):
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle
+
+        t0 = time.perf_counter()
+        work = 0.0
+        done = 0
+        for e in sorted(self.els, key=lambda e: e.n):
+            og = oracle.CSR.from_edgelist(e)
+            k = max(threads, 1) * 2
+            src = np.arange(0, e.n, max(1, e.n // k))[:k].astype(np.int32)
+            oracle.exact_bc_sources(og, src, threads=threads)
+            work += src.size * e.m
+            done += 1
+            if time.perf_counter() - t0 > budget_s:
+                break
+        dt = time.perf_counter() - t0
+        return work / dt / 1e9, dt, f"{2 * max(threads, 1)} sources of each of the {done} smallest graphs"
+
+
+EXTRA_WORKLOADS = {
+    "grid2048-clustered": GridClustered4M,
+    "grid512-exact": lambda: ExactWorkload("grid512-exact", "grid512"),
+    "grid32-exact": lambda: ExactWorkload("grid32-exact", "grid32"),
+    "rgg48-exact": MultiGraph,
+}
+
+
+def run_extra(args):
+    """One of the other configurations (the default bench line is the clustered 256x256 grid)."""
+    import torch
+
+    import fastbc_gpu as fg
+
+    fg.init(0)
+    prec = fg.FP32C if args.prec == "fp32c" else fg.FP64
+    sched = fg.BATCHED if args.sched == "batched" else fg.PLAIN
+    wl = EXTRA_WORKLOADS[args.workload]()
+    wl.setup(fg, args)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    for _ in range(args.warmup):
+        wl.step(fg, prec, sched)
+    dev = wall = 0.0
+    launches = 0
+    kern = {"warp_ms": 0.0, "block_ms": 0.0, "warp_bytes": 0.0, "block_bytes": 0.0}
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        sts = wl.step(fg, prec, sched)
+        wall += time.perf_counter() - t0
+        for st in sts:
+            dev += st.kernel_ms / 1e3
+            launches += st.launches
+            for k in kern:
+                kern[k] += getattr(st, k)
+    dom = "warp" if kern["warp_ms"] >= kern["block_ms"] else "block"
+    achieved = kern[f"{dom}_bytes"] / (kern[f"{dom}_ms"] / 1e3) / 1e9 if kern[f"{dom}_ms"] else 0.0
+    line = {"metric": METRIC, "value": wl.work * args.steps / dev / 1e9, "unit": "GTEPS", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev / args.steps * 1e3,
+            "higher_is_better": True, "dtype": "f32x2+u64" if prec == fg.FP32C else "f64+u64",
+            "config": dict(wl.config, precision=args.prec, schedule=args.sched),
+            "e2e": {"value": wl.work * args.steps / wall / 1e9, "unit": "GTEPS"},
+            "gpu_launches": launches,
+            "roofline": {"kernel": dom, "achieved": achieved, "unit": "GB/s"}}
+    if args.workload in ("grid512-exact", "grid32-exact") and args.prec == "fp32c":
+        wl.step(fg, fg.FP64, sched)
+        ref = wl.last.copy()
+        wl.step(fg, fg.FP32C, sched)
+        got = wl.last
+        nz = ref != 0
+        rel = np.abs(got[nz] - ref[nz]) / np.abs(ref[nz])
+        line["precision_vs_fp64"] = {"max_rel": float(rel.max()), "mean_rel": float(rel.mean()),
+                                     "reference": "the FP64 form on the GPU (parity-tested against the oracle)"}
+    if not args.no_cpu_baseline:
+        v, dt, what = wl.cpu_sample(os.cpu_count() or 1, args.ref_budget)
+        line["cpu_baseline"] = {"value": v, "unit": "GTEPS", "cores": os.cpu_count() or 1, "kind": "port",
+                                "sample": f"{what} in {dt:.1f} s"}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
@@ -193,11 +442,20 @@ def main():
     ap.add_argument("--sched", default="batched", choices=["batched", "plain"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ref-budget", type=float, default=12.0)
+    ap.add_argument("--workload", default="grid256-clustered",
+                    choices=["grid256-clustered"] + sorted(EXTRA_WORKLOADS))
+    ap.add_argument("--fraction", type=float, default=1.0 / 16,
+                    help="grid2048-clustered: fraction of tiles and pivots per step")
+    ap.add_argument("--sequential", action="store_true", help="rgg48-exact: one call per graph")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="batched schedule: keep the default knobs instead of tuning them first")
     ap.add_argument("--small", action="store_true",
                     help="profiling case: 8 clusters and 256 pivots of the same workload")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload != "grid256-clustered":
+        return run_extra(args)
 
     ws, rank, local = dist_env()
     import torch
@@ -232,9 +490,22 @@ def main():
     work = work_per_step(el, z, keep)
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
 
+    tuned = {}
+    if sched == fg.BATCHED and not args.no_autotune:
+        import autotune
+
+        tuned["clusters"] = autotune.tune_clusters(g, cs, prec)
+        tuned["pivots"] = autotune.tune_pivots(g, allp, allc, prec)
+
+    def knobs(phase):
+        for k, v in tuned.get(phase, {}).items():
+            fg.set_option(k, v)
+
     def step():
         st1, st2 = fg.Stats(), fg.Stats()
+        knobs("clusters")
         ev = fg.cluster_eval_batch(g, cs, prec, sched, stats=st1)
+        knobs("pivots")
         bc = fg.dependency_batch(g, allp, allc, prec, sched, out=ev.intra_bc.copy(), stats=st2)
         for c in range(len(clusters)):
             tot = float(np.sum(cards[keep[c]]))
@@ -298,6 +569,7 @@ def main():
                        "graph_seed": 42, "louvain_seeds": [1, 2, 3, 4], "louvain_precision": 0.01,
                        "kfrac": 0.5, "clusters": len(keep), "pivots": int(allp.size),
                        "relaxations_per_step": work, "precision": args.prec, "schedule": args.sched,
+                       "autotuned": tuned,
                        "l2": "flushed (512 MiB write) before every step", "parallelism": f"replicas{ws}"},
             "s_per_graph": tot_dev / args.steps,
             "e2e": {"value": e2e, "unit": "GTEPS", "h2d_bytes_per_step": h2d // args.steps,

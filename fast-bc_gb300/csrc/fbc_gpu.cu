@@ -75,9 +75,10 @@ struct DBuf {
 };
 
 struct Options {
-    int64_t delta = 0;          // bucket width; 0 = mean edge weight of the graph
+    int64_t delta = 0;          // bucket width; 0 = 4 x mean edge weight of the graph
     int64_t block_threads = 256;    // plain schedule
     int64_t frontier_threads = 128; // batched schedule, large segments
+    int64_t chunk_max = 512;        // batched small segments: sources per work item
     int64_t warp_max_n = 4096;  // batched: segments up to this size run one source per warp
     int64_t iter_mult = 16;
     int64_t ws_budget_mb = 0;   // 0 = 60% of the free device memory
@@ -206,7 +207,7 @@ int make_graph(int32_t n, std::vector<int64_t>&& rp, std::vector<int32_t>&& col,
 
 int delta_for(double meanw) {
     if (g.opt.delta > 0) return (int)std::min<int64_t>(g.opt.delta, 0x3fffffff);
-    return std::max(1, (int)std::lround(meanw));
+    return std::max(1, (int)std::lround(4.0 * meanw));
 }
 
 // A batch of work: segments + units, output sizes and debug pointers.
@@ -286,7 +287,7 @@ int launch_block(const Plan& P, const std::vector<Unit>& units, int ws_n, fbc_st
     const int64_t sb = fr ? fbc::fstate_bytes<Prec>(ws_n) : fbc::state_bytes<Prec>(ws_n);
     const int64_t stride = 256 + ((sb + 255) & ~int64_t(255));
     int threads = (int)std::min<int64_t>(std::max<int64_t>(fr ? g.opt.frontier_threads : g.opt.block_threads, 32),
-                                         fr ? 256 : 1024);
+                                         fr ? 128 : 1024);
     threads = (threads / 32) * 32;
     int bps = 0;
     if (fr) FBC_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, fbc::frontier_kernel<Prec>, threads, 0));
@@ -336,8 +337,10 @@ int launch_small(const Plan& P, const std::vector<Unit>& units, int nmax, int mm
         1, std::min<int64_t>(16, (dyn - L.pool) / fbc::SmallLayout::per_warp(std::max(nmin, 1))));
     // chunks: consecutive units of one segment, enough of them to balance the SMs
     std::vector<fbc::Chunk> ch;
+    // large chunks keep the block's warps busy between the barriers that reload the CSR;
+    // about two chunks per block still balance the blocks
     const int64_t per_chunk = std::max<int64_t>(
-        2 * wpb, std::min<int64_t>(256, (int64_t)units.size() / std::max<int64_t>(1, (int64_t)g.nsm * 4)));
+        4 * wpb, std::min<int64_t>(g.opt.chunk_max, (int64_t)units.size() / std::max<int64_t>(1, (int64_t)g.nsm * 2)));
     for (size_t i = 0; i < units.size();) {
         size_t j = i;
         while (j < units.size() && units[j].seg == units[i].seg && (int64_t)(j - i) < per_chunk) ++j;
@@ -615,7 +618,8 @@ int fbc_set_option(const char* key, int64_t value) {
     std::string k(key);
     if (k == "delta") g.opt.delta = std::max<int64_t>(0, value);
     else if (k == "block_threads") g.opt.block_threads = std::max<int64_t>(32, std::min<int64_t>(1024, value));
-    else if (k == "frontier_threads") g.opt.frontier_threads = std::max<int64_t>(32, std::min<int64_t>(256, value));
+    else if (k == "chunk_max") g.opt.chunk_max = std::max<int64_t>(1, value);
+    else if (k == "frontier_threads") g.opt.frontier_threads = std::max<int64_t>(32, std::min<int64_t>(128, value));
     else if (k == "warp_max_n") g.opt.warp_max_n = std::max<int64_t>(0, value);
     else if (k == "iter_mult") g.opt.iter_mult = std::max<int64_t>(1, std::min<int64_t>(1 << 20, value));
     else if (k == "ws_budget_mb") g.opt.ws_budget_mb = std::max<int64_t>(0, value);
@@ -631,6 +635,7 @@ int fbc_get_option(const char* key, int64_t* value) {
     std::string k(key);
     if (k == "delta") *value = g.opt.delta;
     else if (k == "block_threads") *value = g.opt.block_threads;
+    else if (k == "chunk_max") *value = g.opt.chunk_max;
     else if (k == "frontier_threads") *value = g.opt.frontier_threads;
     else if (k == "warp_max_n") *value = g.opt.warp_max_n;
     else if (k == "iter_mult") *value = g.opt.iter_mult;

@@ -23,10 +23,13 @@ namespace fbc {
 struct QEnt {
     int v, e0, deg, pad;
 };
-// A vertex of a Kahn level: distance, final path count and row.
+// A vertex of a Kahn level: distance, final path count, row, and (written when the vertex's
+// level is processed) the mask of its tight out-edges, so that the dependency pass reads only
+// those.  Rows longer than 32 edges set the mask to all ones and re-test tightness.
 struct LEnt {
     int v, d, e0, deg;
     unsigned long long sig;
+    unsigned tmask, pad;
 };
 
 template <class Prec>
@@ -268,7 +271,7 @@ __device__ void frontier_unit(const KParams& P, int64_t ui, const Unit& u, const
         }
         if (tid == 0) {
             const int e0 = __ldg(rp + src);
-            S.order[0] = LEnt{src, 0, e0, __ldg(rp + src + 1) - e0, 1ull};
+            S.order[0] = LEnt{src, 0, e0, __ldg(rp + src + 1) - e0, 1ull, 0u, 0u};
             S.lvl[0] = 0;
             C.ocnt = 1;
         }
@@ -278,13 +281,14 @@ __device__ void frontier_unit(const KParams& P, int64_t ui, const Unit& u, const
             if (nlev >= n) { bad = kErrIter; break; }
             for (int base = lo + (tid & ~31); base < hi; base += nth) {
                 const int i = base + (tid & 31);
-                int e = 0, e1 = 0, dv = 0;
+                int e = 0, e1 = 0, dv = 0, e0 = 0;
                 unsigned long long sv = 0;
+                unsigned tmask = 0u;
                 if (i < hi) {
                     const LEnt o = S.order[i];
                     dv = o.d;
                     sv = o.sig;
-                    e = o.e0;
+                    e = e0 = o.e0;
                     e1 = o.e0 + o.deg;
                 }
                 while (__any_sync(kFull, e < e1)) {
@@ -305,8 +309,10 @@ __device__ void frontier_unit(const KParams& P, int64_t ui, const Unit& u, const
 #pragma unroll
                     for (int k = 0; k < 4; ++k) {
                         bool push = false;
-                        LEnt le{x[k], nd[k], 0, 0, 0ull};
+                        LEnt le{x[k], nd[k], 0, 0, 0ull, 0u, 0u};
                         if (tight[k]) {
+                            const int bit = e + k - e0;
+                            tmask |= bit < 32 ? (1u << bit) : 0xffffffffu;
                             // one atomic adds sigma_v and retires the edge; the thread that
                             // retires the last tight in-edge knows x's final count
                             const unsigned long long old = atomicAdd(S.sc + x[k], (sv << 16) - 1ull);
@@ -321,6 +327,7 @@ __device__ void frontier_unit(const KParams& P, int64_t ui, const Unit& u, const
                     }
                     e += 4;
                 }
+                if (i < hi) S.order[i].tmask = e1 - e0 > 32 ? 0xffffffffu : tmask;
             }
             __syncthreads();
             ++nlev;
@@ -349,36 +356,45 @@ __device__ void frontier_unit(const KParams& P, int64_t ui, const Unit& u, const
                 const int v = o.v, dv = o.d;
                 const unsigned long long sv = o.sig;
                 typename Prec::Acc acc = Prec::zero();
-                const int e1 = o.e0 + o.deg;
-                for (int e = o.e0; e < e1; e += 4) {
-                    int x[4], nd[4];
+                if (o.deg <= 32) {
+                    // tight out-edges only, four at a time (the mask was set by the Kahn pass)
+                    unsigned mk = o.tmask;
+                    while (mk) {
+                        int x[4];
 #pragma unroll
-                    for (int k = 0; k < 4; ++k) {
-                        x[k] = -1;
-                        if (e + k < e1) {
-                            const int2 a = __ldg(adj + e + k);
-                            x[k] = a.x;
-                            nd[k] = dv + a.y;
+                        for (int k = 0; k < 4; ++k) {
+                            x[k] = -1;
+                            if (mk) {
+                                const int b = __ffs(mk) - 1;
+                                mk &= mk - 1u;
+                                x[k] = __ldg(adj + o.e0 + b).x;
+                            }
+                        }
+                        unsigned long long sx[4];
+                        typename Prec::D dx[4];
+#pragma unroll
+                        for (int k = 0; k < 4; ++k)
+                            if (x[k] >= 0) {
+                                sx[k] = __ldcg(S.sc + x[k]) >> 16;
+                                dx[k] = S.dlt[x[k]];
+                            }
+#pragma unroll
+                        for (int k = 0; k < 4; ++k)
+                            if (x[k] >= 0) {
+                                if (sx[k] == sv) Prec::add_same(acc, dx[k]);
+                                else Prec::add(acc, sv, sx[k], dx[k]);
+                            }
+                    }
+                } else {
+                    const int e1 = o.e0 + o.deg;
+                    for (int e = o.e0; e < e1; ++e) {
+                        const int2 a = __ldg(adj + e);
+                        if (dv + a.y == dist_of(ldcg64(S.word + a.x))) {
+                            const unsigned long long sx = __ldcg(S.sc + a.x) >> 16;
+                            if (sx == sv) Prec::add_same(acc, S.dlt[a.x]);
+                            else Prec::add(acc, sv, sx, S.dlt[a.x]);
                         }
                     }
-                    bool tight[4];
-                    unsigned long long sx[4];
-                    typename Prec::D dx[4];
-#pragma unroll
-                    for (int k = 0; k < 4; ++k) {
-                        tight[k] = false;
-                        if (x[k] >= 0) {
-                            tight[k] = nd[k] == dist_of(ldcg64(S.word + x[k]));
-                            sx[k] = __ldcg(S.sc + x[k]) >> 16;
-                            dx[k] = S.dlt[x[k]];
-                        }
-                    }
-#pragma unroll
-                    for (int k = 0; k < 4; ++k)
-                        if (tight[k]) {
-                            if (sx[k] == sv) Prec::add_same(acc, dx[k]);
-                            else Prec::add(acc, sv, sx[k], dx[k]);
-                        }
                 }
                 S.dlt[v] = Prec::store(acc);
                 if (v != src) {
@@ -416,7 +432,7 @@ __device__ void frontier_unit(const KParams& P, int64_t ui, const Unit& u, const
 }
 
 template <class Prec>
-__global__ void __launch_bounds__(256, 2) frontier_kernel(KParams P) {
+__global__ void __launch_bounds__(128, 5) frontier_kernel(KParams P) {
     __shared__ FCtl C;
     char* slot = P.ws + (int64_t)blockIdx.x * P.ws_stride;
     unsigned* hdr = (unsigned*)slot;

@@ -280,3 +280,58 @@ def test_rgg_sources_bit_exact_batched(fg):
             check_source(fg, g, og, src)
     finally:
         fg.set_option("debug_sched", 0)
+
+
+def test_rgg_batch_smallest_graphs(fg):
+    """The 48-graph batching workload: its four smallest graphs, exact BC against the oracle."""
+    els = sorted(graphs.rgg_batch(48), key=lambda e: e.n)[:4]
+    gs = [fg.Graph.from_edgelist(e) for e in els]
+    for prec, tol in ((fg.FP64, TOL_FP64), (fg.FP32C, TOL_FP32C)):
+        for sched in (fg.PLAIN, fg.BATCHED):
+            outs = fg.multi_exact_bc(gs, prec, sched)
+            for e, o in zip(els, outs):
+                assert rel_err(o, oracle.exact_bc(oracle.CSR.from_edgelist(e))) <= tol
+
+
+def test_grid512_precision_form(fg):
+    """Precision configuration (512x512 grid): on 512 sampled sources the FP32-compensated form
+    stays within 1e-6 of the FP64 form (itself within 1e-9 of the oracle on a subset), and
+    distances and path counts are bit-exact."""
+    el = graphs.WORKLOADS["grid512"]()
+    og = oracle.CSR.from_edgelist(el)
+    g = fg.Graph.from_edgelist(el)
+    src = np.unique(graphs.rand_int(5, 1, np.arange(512), 0, el.n - 1)).astype(np.int32)
+    f64 = fg.dependency_batch(g, src, None, fg.FP64, fg.BATCHED)
+    f32 = fg.dependency_batch(g, src, None, fg.FP32C, fg.BATCHED)
+    assert rel_err(f32, f64) <= TOL_FP32C
+    ref = oracle.exact_bc_sources(og, src[:8], threads=8)
+    got = fg.dependency_batch(g, src[:8], None, fg.FP64, fg.BATCHED)
+    assert rel_err(got, ref) <= TOL_FP64
+    fg.set_option("debug_sched", 1)
+    try:
+        check_source(fg, g, og, int(src[0]))
+    finally:
+        fg.set_option("debug_sched", 0)
+
+
+def test_grid2048_full_size_sources(fg):
+    """Full form graph (4,194,304 vertices): two sources bit-exact against the oracle through both
+    block kernels, and FP32C vs FP64 on 32 sampled sources."""
+    el = graphs.WORKLOADS["grid2048"]()
+    og = oracle.CSR.from_edgelist(el)
+    g = fg.Graph.from_edgelist(el)
+    for sched, s in ((0, 1234567), (1, el.n - 1)):
+        fg.set_option("debug_sched", sched)
+        try:
+            dist, sig, dlt, npred = fg.sssp_debug(g, s)
+        finally:
+            fg.set_option("debug_sched", 0)
+        od, osg, odl, order, preds = oracle.sssp_dump(og, s)
+        assert np.array_equal(np.where(dist < 0, np.inf, dist.astype(np.float64)), od)
+        assert np.array_equal(sig.astype(np.float64), osg)
+        assert np.array_equal(npred, np.array([len(p) for p in preds]))
+        assert rel_err(dlt[od < np.inf], odl[od < np.inf]) <= TOL_FP64
+    src = np.arange(7, el.n, el.n // 32, dtype=np.int32)[:32]
+    f64 = fg.dependency_batch(g, src, None, fg.FP64, fg.BATCHED)
+    f32 = fg.dependency_batch(g, src, None, fg.FP32C, fg.BATCHED)
+    assert rel_err(f32, f64) <= TOL_FP32C
