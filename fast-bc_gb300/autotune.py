@@ -39,10 +39,11 @@ def _apply(choice: dict) -> dict:
     return choice
 
 
-def tune_pivots(g: fg.Graph, sources, cards=None, precision: int = fg.FP32C, sample: int = 1024,
-                deltas=(2, 4, 8), threads=(96, 128)) -> dict:
+def tune_pivots(g: fg.Graph, sources, cards=None, precision: int = fg.FP32C, sample: int = 4096,
+                deltas=(2, 4, 8), threads=(96, 128, 512)) -> dict:
     """Whole-graph sources (pivots, exact mode): delta (as multiples of the mean weight) and
-    the frontier kernel's block size, on an evenly spaced sample of the sources."""
+    the frontier kernel's block size.  Up to `sample` sources the whole list is timed, so the
+    number of waves over the concurrent slots (which the block size sets) is the real one."""
     src = np.asarray(sources, np.int32)
     idx = np.linspace(0, src.size - 1, min(sample, src.size)).astype(np.int64)
     s = src[idx]

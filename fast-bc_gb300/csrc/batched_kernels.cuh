@@ -313,7 +313,10 @@ __device__ void small_unit(const KParams& K, const Seg& sg, const Unit& u, const
             __syncwarp();
         }
     }
-    if (bad && lane == 0) atomicOr(K.err, bad);
+    if (bad && lane == 0) {
+        if (bad == kErrSigma) request_retry(K, u, kErrSigma);  // recomputed with FP64 counts
+        else atomicOr(K.err, bad);
+    }
     __syncwarp();
 }
 

@@ -40,7 +40,7 @@ namespace fbc {
 constexpr int32_t kInf = 0x7fffffff;
 constexpr unsigned kFull = 0xffffffffu;
 
-enum : int { kErrIter = 1, kErrSigma = 2, kErrQueue = 4 };
+enum : int { kErrIter = 1, kErrSigma = 2, kErrQueue = 4, kErrRetry = 8 };
 
 // One CSR segment (device pointers).
 struct Seg {
@@ -63,6 +63,16 @@ struct Unit {
     int64_t bout;    // first border-output entry of this source, or -1
 };
 
+// A unit whose path counts outgrew the kernel's representation.  It stopped before its
+// dependency pass (nothing accumulated) and the host recomputes it one level up:
+// code kErrRetry -> plain kernel with 64-bit counts, kErrSigma -> plain kernel with FP64
+// counts (the reference's own representation, exact below 2^53).
+struct RetryRec {
+    Unit u;
+    int32_t code;
+    int32_t pad;
+};
+
 struct KParams {
     const Seg* segs;
     const Unit* units;
@@ -76,13 +86,24 @@ struct KParams {
     int64_t ws_stride;
     int32_t ws_n;                // capacity (vertices) of one slot / one shared-memory state
     int32_t iter_mult;           // distance-pass round cap = iter_mult * (n + 2)
-    int* retry_count;            // units to recompute on the plain kernel (batched only)
-    int* retry;
+    int* retry_count;            // units to recompute one level up (null: report an error)
+    RetryRec* retry;
     int32_t retry_cap;
     int32_t* dbg_dist;           // debug dump of one unit (may be null)
     unsigned long long* dbg_sig;
     double* dbg_dlt;
 };
+
+// Hand a unit back to the host (see RetryRec); without a retry list, report the error.
+__device__ __forceinline__ void request_retry(const KParams& P, const Unit& u, int code) {
+    if (!P.retry) {
+        atomicOr(P.err, code == kErrRetry ? kErrSigma : code);
+        return;
+    }
+    const int r = atomicAdd(P.retry_count, 1);
+    if (r < P.retry_cap) P.retry[r] = RetryRec{u, code, 0};
+    else atomicOr(P.err, kErrQueue);
+}
 
 // ----------------------------------------------------------------------------- groups
 struct BlockGroup {
@@ -113,8 +134,10 @@ struct PrecF64 {
     struct Acc { double s; };
     __device__ static Acc zero() { return {0.0}; }
     // ExactBrandesBC.h:81: sigma[v] / sigma[w] * (1.0 + delta[w]), division first
-    __device__ static void add(Acc& a, unsigned long long sv, unsigned long long sw, D dw) {
-        a.s += (double)sv / (double)sw * (1.0 + dw);
+    // path counts arrive as doubles: exact below 2^53, where the reference's double counts
+    // are exact too
+    __device__ static void add(Acc& a, double sv, double sw, D dw) {
+        a.s += sv / sw * (1.0 + dw);
     }
     // sigma_v == sigma_w: the ratio is exactly 1.0 and 1.0 * y == y
     __device__ static void add_same(Acc& a, D dw) { a.s += 1.0 + dw; }
@@ -138,15 +161,15 @@ struct PrecDF32 {
         s = __fadd_rn(a, b);
         e = __fsub_rn(b, __fsub_rn(s, a));
     }
-    __device__ static void add(Acc& a, unsigned long long sv, unsigned long long sw, D dw) {
+    __device__ static void add(Acc& a, double sv, double sw, D dw) {
         // ratio r = sv / sw as a double-float
         float rh, rl;
-        if (sv <= (1ull << 24) && sw <= (1ull << 24)) {
+        if (sv <= 16777216.0 && sw <= 16777216.0) {
             float x = (float)sv, y = (float)sw;   // exact
             rh = __fdiv_rn(x, y);
             rl = __fdiv_rn(__fmaf_rn(-rh, y, x), y);  // the remainder x - rh*y is exact
         } else {
-            double rd = (double)sv / (double)sw;  // FP64 only above 2^24
+            double rd = sv / sw;  // FP64 only above 2^24
             rh = __double2float_rn(rd);
             rl = __double2float_rn(rd - (double)rh);
         }
@@ -275,6 +298,7 @@ struct Ctl {
     int ocnt;
     int unit;
     unsigned epoch;
+    int sbad;        // path-count overflow seen by any thread of the unit
 };
 
 // Fill a state with the invariant values (all cap entries).
@@ -290,8 +314,42 @@ __device__ void state_init(const State<Prec>& s, int cap) {
     G::sync();
 }
 
+// Path counts: uint64 (exact; overflow hands the unit back for FP64 counts) or FP64 (the
+// reference's own representation), in the same 8-byte array.
+template <bool kF64>
+__device__ __forceinline__ double sig_val(unsigned long long bits) {
+    if constexpr (kF64) return __longlong_as_double((long long)bits);
+    else return (double)bits;
+}
+template <bool kF64>
+__device__ __forceinline__ unsigned long long sig_one() {
+    if constexpr (kF64) return (unsigned long long)__double_as_longlong(1.0);
+    else return 1ull;
+}
+// adds the count of a predecessor (raw bits); true when a uint64 count overflowed
+template <bool kF64>
+__device__ __forceinline__ bool sig_add_g(unsigned long long* p, unsigned long long a) {
+    if constexpr (kF64) {
+        atomicAdd((double*)p, __longlong_as_double((long long)a));
+        return false;
+    } else {
+        const unsigned long long old = atomicAdd(p, a);
+        return old + a < old;
+    }
+}
+// uint64 border/debug output of a count (FP64 counts saturate at 2^64 - 1)
+template <bool kF64>
+__device__ __forceinline__ unsigned long long sig_out(unsigned long long bits) {
+    if constexpr (kF64) {
+        const double d = __longlong_as_double((long long)bits);
+        return d >= 18446744073709551615.0 ? ~0ull : (unsigned long long)d;
+    } else {
+        return bits;
+    }
+}
+
 // ---------------------------------------------------------------------- one unit
-template <class G, class Prec>
+template <class G, class Prec, bool kSigF64 = false>
 __device__ void run_unit(const KParams& P, const Unit& u, const State<Prec>& S, Ctl& C,
                          unsigned& epoch, int cap) {
     constexpr bool kSh = G::kShared;
@@ -319,9 +377,10 @@ __device__ void run_unit(const KParams& P, const Unit& u, const State<Prec>& S, 
     unsigned fgen = ++epoch;
     if (G::rank() == 0) {
         S.dist[src] = 0;
-        S.sig[src] = 1ull;
+        S.sig[src] = sig_one<kSigF64>();
         S.q[0][0] = src;
         S.nflag[src] = epoch + 1;
+        C.sbad = 0;
         C.ncnt[0] = 1;
         C.ncnt[1] = 0;
         C.fcnt[0] = 0;
@@ -467,8 +526,7 @@ __device__ void run_unit(const KParams& P, const Unit& u, const State<Prec>& S, 
                         const int2 a = __ldg(adj + ev);
                         x = a.x;
                         if (dvv + a.y == ld_i32<kSh>(S.dist + x)) {
-                            const unsigned long long old = atomicAdd(S.sig + x, svv);
-                            if (old + svv < old) atomicOr(P.err, kErrSigma);
+                            if (sig_add_g<kSigF64>(S.sig + x, svv)) C.sbad = 1;
                             push = atomicSub(S.cnt + x, 1) == 1;
                         }
                     }
@@ -483,15 +541,18 @@ __device__ void run_unit(const KParams& P, const Unit& u, const State<Prec>& S, 
             G::sync();
         }
         reached = hi;
+        G::sync();
+        const bool overflow = C.sbad != 0;  // uint64 counts overflowed: retry with FP64 counts
+        if (overflow) bad = kErrSigma;
 
         // border (dist or 0 when unreached, sigma) of this source: DijkstraClusterEvaluator.h:166-177
-        if (u.bout >= 0) {
+        if (!overflow && u.bout >= 0) {
             const int* bl = sg.border;
             for (int j = G::rank(); j < sg.nb; j += G::size()) {
                 const int b = bl[j];
                 const int d = ld_i32<kSh>(S.dist + b);
                 P.bdist[u.bout + j] = d != kInf ? (double)d : 0.0;
-                P.bsig[u.bout + j] = ld_u64<kSh>(S.sig + b);
+                P.bsig[u.bout + j] = sig_out<kSigF64>(ld_u64<kSh>(S.sig + b));
             }
         }
     }
@@ -504,13 +565,15 @@ __device__ void run_unit(const KParams& P, const Unit& u, const State<Prec>& S, 
             for (int i = a0 + G::rank(); i < a1; i += G::size()) {
                 const int v = order[i];
                 const int dv = ld_i32<kSh>(S.dist + v);
-                const unsigned long long sv = ld_u64<kSh>(S.sig + v);
+                const double sv = sig_val<kSigF64>(ld_u64<kSh>(S.sig + v));
                 typename Prec::Acc acc = Prec::zero();
                 const int e1 = rp[v + 1];
                 for (int e = rp[v]; e < e1; ++e) {
                     const int2 a = __ldg(adj + e);
                     if (dv + a.y == ld_i32<kSh>(S.dist + a.x)) {
-                        Prec::add(acc, sv, ld_u64<kSh>(S.sig + a.x), S.dlt[a.x]);
+                        const double sx = sig_val<kSigF64>(ld_u64<kSh>(S.sig + a.x));
+                        if (sx == sv) Prec::add_same(acc, S.dlt[a.x]);
+                        else Prec::add(acc, sv, sx, S.dlt[a.x]);
                     }
                 }
                 S.dlt[v] = Prec::store(acc);
@@ -523,12 +586,15 @@ __device__ void run_unit(const KParams& P, const Unit& u, const State<Prec>& S, 
         }
     }
     (void)reached;
-    if (bad && G::rank() == 0) atomicOr(P.err, bad);
+    if (bad && G::rank() == 0) {
+        if (bad == kErrSigma) request_retry(P, u, kErrSigma);
+        else atomicOr(P.err, bad);
+    }
     if (P.dbg_dist) {
         for (int v = G::rank(); v < n; v += G::size()) {
             const int d = ld_i32<kSh>(S.dist + v);
             P.dbg_dist[v] = d != kInf ? d : -1;
-            P.dbg_sig[v] = ld_u64<kSh>(S.sig + v);
+            P.dbg_sig[v] = sig_out<kSigF64>(ld_u64<kSh>(S.sig + v));
             P.dbg_dlt[v] = d != kInf ? Prec::value(Prec::load(S.dlt[v])) : 0.0;
         }
         G::sync();
@@ -546,7 +612,7 @@ __device__ void run_unit(const KParams& P, const Unit& u, const State<Prec>& S, 
 // ------------------------------------------------------------------------- kernels
 // Block per source, state in a global-memory slot per block; blocks pull units from a
 // shared counter until none are left (persistent grid, sized by the host).
-template <class Prec>
+template <class Prec, bool kSigF64 = false>
 __global__ void __launch_bounds__(1024) brandes_block_kernel(KParams P) {
     __shared__ Ctl C;
     char* slot = P.ws + (int64_t)blockIdx.x * P.ws_stride;
@@ -564,7 +630,7 @@ __global__ void __launch_bounds__(1024) brandes_block_kernel(KParams P) {
         __syncthreads();
         if (ui >= P.nunits) break;
         const Unit u = P.units[ui];
-        run_unit<BlockGroup, Prec>(P, u, S, C, epoch, P.ws_n);
+        run_unit<BlockGroup, Prec, kSigF64>(P, u, S, C, epoch, P.ws_n);
     }
     if (threadIdx.x == 0) hdr[0] = epoch;
 }

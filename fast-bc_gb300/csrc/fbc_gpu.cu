@@ -79,6 +79,7 @@ struct Options {
     int64_t block_threads = 256;    // plain schedule
     int64_t frontier_threads = 128; // batched schedule, large segments
     int64_t chunk_max = 512;        // batched small segments: sources per work item
+    int64_t wide_n = 1 << 20;       // batched large segments: 512-thread blocks from this size
     int64_t warp_max_n = 4096;  // batched: segments up to this size run one source per warp
     int64_t iter_mult = 16;
     int64_t ws_budget_mb = 0;   // 0 = 60% of the free device memory
@@ -247,8 +248,8 @@ KParams base_params(const Plan& P) {
     K.bsig = g.bsig.as<unsigned long long>();
     K.err = (int*)(g.ctr.as<unsigned long long>() + 2);
     K.retry_count = K.err + 1;
-    K.retry = g.retry.as<int>();
-    K.retry_cap = (int32_t)(g.retry.cap / sizeof(int));
+    K.retry = g.retry.as<fbc::RetryRec>();
+    K.retry_cap = (int32_t)(g.retry.cap / sizeof(fbc::RetryRec));
     K.iter_mult = (int32_t)g.opt.iter_mult;
     K.dbg_dist = P.dbg_dist;
     K.dbg_sig = P.dbg_sig;
@@ -256,10 +257,10 @@ KParams base_params(const Plan& P) {
     return K;
 }
 
-// (Re)size a workspace for `slots` slots of `stride` bytes; reuse it when it already fits.
+// (Re)size a workspace for `slots` slots of at least `ws_n` vertices; reuse it when it
+// already fits (then the existing, possibly larger, capacity and stride are used).
 int ensure_ws(Workspace& W, int64_t slots, int64_t stride, int ws_n, int dsize) {
-    if (W.buf.p && W.stride == stride && W.ws_n == ws_n && W.dsize == dsize && W.slots >= slots)
-        return FBC_OK;
+    if (W.buf.p && W.ws_n >= ws_n && W.dsize == dsize && W.slots >= slots) return FBC_OK;
     W.buf.release();
     FBC_CK(W.buf.ensure((size_t)(slots * stride), true));
     W.stride = stride;
@@ -281,16 +282,21 @@ int64_t ws_budget() {
 // batched schedule: frontier_kernel.
 template <class Prec>
 int launch_block(const Plan& P, const std::vector<Unit>& units, int ws_n, fbc_stats* st,
-                 int& launches, bool force_plain = false) {
+                 int& launches, bool force_plain = false, bool sig_f64 = false) {
     if (units.empty()) return FBC_OK;
-    const bool fr = P.sched == FBC_SCHED_BATCHED && !force_plain;
+    const bool fr = P.sched == FBC_SCHED_BATCHED && !force_plain && !sig_f64;
+    // wide blocks for segments of millions of vertices (their frontiers are hundreds wide)
+    const bool wide = fr && (g.opt.frontier_threads > 128 || (int64_t)ws_n >= g.opt.wide_n);
     const int64_t sb = fr ? fbc::fstate_bytes<Prec>(ws_n) : fbc::state_bytes<Prec>(ws_n);
     const int64_t stride = 256 + ((sb + 255) & ~int64_t(255));
     int threads = (int)std::min<int64_t>(std::max<int64_t>(fr ? g.opt.frontier_threads : g.opt.block_threads, 32),
                                          fr ? 128 : 1024);
+    if (wide) threads = 512;
     threads = (threads / 32) * 32;
     int bps = 0;
-    if (fr) FBC_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, fbc::frontier_kernel<Prec>, threads, 0));
+    if (wide) FBC_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, fbc::frontier_kernel<Prec, true>, threads, 0));
+    else if (fr) FBC_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, fbc::frontier_kernel<Prec, false>, threads, 0));
+    else if (sig_f64) FBC_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, fbc::brandes_block_kernel<Prec, true>, threads, 0));
     else FBC_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, fbc::brandes_block_kernel<Prec>, threads, 0));
     bps = std::max(bps, 1);
     int64_t slots = std::min<int64_t>((int64_t)g.nsm * bps, (int64_t)units.size());
@@ -307,9 +313,11 @@ int launch_block(const Plan& P, const std::vector<Unit>& units, int ws_n, fbc_st
     K.nunits = (int64_t)units.size();
     K.next_unit = g.ctr.as<unsigned long long>() + 0;
     K.ws = W.buf.as<char>();
-    K.ws_stride = stride;
-    K.ws_n = ws_n;
-    if (fr) fbc::frontier_kernel<Prec><<<(unsigned)slots, threads, 0, g.st>>>(K);
+    K.ws_stride = W.stride;
+    K.ws_n = W.ws_n;
+    if (wide) fbc::frontier_kernel<Prec, true><<<(unsigned)slots, threads, 0, g.st>>>(K);
+    else if (fr) fbc::frontier_kernel<Prec, false><<<(unsigned)slots, threads, 0, g.st>>>(K);
+    else if (sig_f64) fbc::brandes_block_kernel<Prec, true><<<(unsigned)slots, threads, 0, g.st>>>(K);
     else fbc::brandes_block_kernel<Prec><<<(unsigned)slots, threads, 0, g.st>>>(K);
     FBC_CK(cudaGetLastError());
     ++launches;
@@ -448,24 +456,36 @@ int run_plan_t(Plan& P, fbc_stats* st) {
             }
     int launches = 0;
     FBC_CK(cudaEventRecord(g.ev0, g.st));
-    FBC_CK(g.retry.ensure(sizeof(int) * std::max<size_t>(ub.size(), 1)));
+    FBC_CK(g.retry.ensure(sizeof(fbc::RetryRec) * std::max<size_t>(P.units.size(), 1)));
     FBC_TRY(launch_small<Prec>(P, uw, nw_max, mw_max, nw_min, st, launches));
     FBC_CK(cudaEventRecord(g.evm, g.st));
     FBC_TRY(launch_block<Prec>(P, ub, nb_max, st, launches));
     int err[2] = {0, 0};
     FBC_CK(cudaMemcpyAsync(err, (char*)g.ctr.p + 16, 2 * sizeof(int), cudaMemcpyDeviceToHost, g.st));
     FBC_CK(cudaStreamSynchronize(g.st));
-    if (err[1] > 0 && err[0] == 0) {
-        // units whose path counts outgrew the batched kernel's 48-bit field: recompute them
-        // with the plain kernel (64-bit counts); nothing of theirs was accumulated yet
-        std::vector<int> idx((size_t)err[1]);
-        FBC_CK(cudaMemcpy(idx.data(), g.retry.p, sizeof(int) * idx.size(), cudaMemcpyDeviceToHost));
-        std::vector<Unit> again;
-        for (int i : idx) again.push_back(ub[(size_t)i]);
+    // Units whose path counts outgrew their kernel's representation stopped before their
+    // dependency pass (nothing of theirs was accumulated): recompute them one level up,
+    // 48-bit packed -> 64-bit (plain kernel) -> FP64 counts (plain kernel).
+    for (int round = 0; round < 3 && err[0] == 0 && err[1] > 0; ++round) {
+        std::vector<fbc::RetryRec> rec((size_t)err[1]);
+        FBC_CK(cudaMemcpy(rec.data(), g.retry.p, sizeof(fbc::RetryRec) * rec.size(), cudaMemcpyDeviceToHost));
+        std::vector<Unit> to64, tof64;
+        int nmax = 0;
+        for (const auto& r : rec) {
+            (r.code == fbc::kErrRetry ? to64 : tof64).push_back(r.u);
+            nmax = std::max(nmax, P.segs[r.u.seg].n);
+        }
         FBC_CK(cudaMemsetAsync(g.ctr.p, 0, 8, g.st));
-        FBC_TRY(launch_block<Prec>(P, again, nb_max, st, launches, true));
-        FBC_CK(cudaMemcpyAsync(err, (char*)g.ctr.p + 16, sizeof(int), cudaMemcpyDeviceToHost, g.st));
+        FBC_CK(cudaMemsetAsync((char*)g.ctr.p + 20, 0, 4, g.st));
+        FBC_TRY(launch_block<Prec>(P, to64, nmax, st, launches, true, false));
+        if (!to64.empty() && !tof64.empty()) {
+            FBC_CK(cudaMemsetAsync(g.ctr.p, 0, 8, g.st));
+        }
+        FBC_TRY(launch_block<Prec>(P, tof64, nmax, st, launches, true, true));
+        FBC_CK(cudaMemcpyAsync(err, (char*)g.ctr.p + 16, 2 * sizeof(int), cudaMemcpyDeviceToHost, g.st));
+        FBC_CK(cudaStreamSynchronize(g.st));
     }
+    if (err[0] == 0 && err[1] > 0) err[0] = fbc::kErrSigma;
     FBC_CK(cudaEventRecord(g.ev1, g.st));
     FBC_CK(cudaStreamSynchronize(g.st));
     int errv = err[0];
@@ -619,7 +639,8 @@ int fbc_set_option(const char* key, int64_t value) {
     if (k == "delta") g.opt.delta = std::max<int64_t>(0, value);
     else if (k == "block_threads") g.opt.block_threads = std::max<int64_t>(32, std::min<int64_t>(1024, value));
     else if (k == "chunk_max") g.opt.chunk_max = std::max<int64_t>(1, value);
-    else if (k == "frontier_threads") g.opt.frontier_threads = std::max<int64_t>(32, std::min<int64_t>(128, value));
+    else if (k == "wide_n") g.opt.wide_n = std::max<int64_t>(1, value);
+    else if (k == "frontier_threads") g.opt.frontier_threads = std::max<int64_t>(32, std::min<int64_t>(512, value));
     else if (k == "warp_max_n") g.opt.warp_max_n = std::max<int64_t>(0, value);
     else if (k == "iter_mult") g.opt.iter_mult = std::max<int64_t>(1, std::min<int64_t>(1 << 20, value));
     else if (k == "ws_budget_mb") g.opt.ws_budget_mb = std::max<int64_t>(0, value);
@@ -636,6 +657,7 @@ int fbc_get_option(const char* key, int64_t* value) {
     if (k == "delta") *value = g.opt.delta;
     else if (k == "block_threads") *value = g.opt.block_threads;
     else if (k == "chunk_max") *value = g.opt.chunk_max;
+    else if (k == "wide_n") *value = g.opt.wide_n;
     else if (k == "frontier_threads") *value = g.opt.frontier_threads;
     else if (k == "warp_max_n") *value = g.opt.warp_max_n;
     else if (k == "iter_mult") *value = g.opt.iter_mult;

@@ -23,21 +23,29 @@ namespace fbc {
 struct QEnt {
     int v, e0, deg, pad;
 };
-// A vertex of a Kahn level: distance, final path count, row, and (written when the vertex's
-// level is processed) the mask of its tight out-edges, so that the dependency pass reads only
-// those.  Rows longer than 32 edges set the mask to all ones and re-test tightness.
+// A vertex of a Kahn level: distance, row start, final path count, and `dm`: the row length
+// until the vertex's own level is processed, then the mask of its tight out-edges, so that the
+// dependency pass reads only those (all ones: re-test every edge of the row).
 struct LEnt {
-    int v, d, e0, deg;
+    int v, d, e0;
+    unsigned dm;
     unsigned long long sig;
-    unsigned tmask, pad;
 };
+
+// Near queues and far piles hold a vertex at most once each, but the frontiers of road-like
+// graphs are far smaller than n: they get qcap entries, and a unit that would overflow them is
+// handed to the plain kernel (whose queues hold n).
+__host__ __device__ inline int64_t fqcap(int64_t cap) {
+    const int64_t q = cap / 4 + 1 > 65536 ? cap / 4 + 1 : 65536;
+    return q < cap + 1 ? q : cap + 1;
+}
 
 template <class Prec>
 struct FState {
     unsigned long long* word;     // (dist << 32 | queue stamp)
     unsigned long long* sc;       // (sigma << 16 | tight in-edges still unprocessed)
     typename Prec::D* dlt;
-    QEnt* q[4];                   // near0, near1, far0, far1 (cap + 1 entries)
+    QEnt* q[4];                   // near0, near1, far0, far1 (fqcap(cap) entries)
     LEnt* order;                  // cap + 1 entries
     int* lvl;                     // cap + 1 entries
 };
@@ -46,7 +54,7 @@ template <class Prec>
 __host__ __device__ inline int64_t fstate_bytes(int64_t cap) {
     auto al = [](int64_t x) { return (x + 255) & ~int64_t(255); };
     return al(cap * 8) + al(cap * 8) + al(cap * (int64_t)sizeof(typename Prec::D)) +
-           4 * al((cap + 1) * (int64_t)sizeof(QEnt)) + al((cap + 1) * (int64_t)sizeof(LEnt)) +
+           4 * al(fqcap(cap) * (int64_t)sizeof(QEnt)) + al((cap + 1) * (int64_t)sizeof(LEnt)) +
            al((cap + 1) * 4);
 }
 
@@ -57,7 +65,7 @@ __device__ inline FState<Prec> fstate_carve(char* p, int64_t cap) {
     s.word = (unsigned long long*)p; p += al(cap * 8);
     s.sc = (unsigned long long*)p; p += al(cap * 8);
     s.dlt = (typename Prec::D*)p; p += al(cap * (int64_t)sizeof(typename Prec::D));
-    for (int i = 0; i < 4; ++i) { s.q[i] = (QEnt*)p; p += al((cap + 1) * (int64_t)sizeof(QEnt)); }
+    for (int i = 0; i < 4; ++i) { s.q[i] = (QEnt*)p; p += al(fqcap(cap) * (int64_t)sizeof(QEnt)); }
     s.order = (LEnt*)p; p += al((cap + 1) * (int64_t)sizeof(LEnt));
     s.lvl = (int*)p;
     return s;
@@ -69,19 +77,21 @@ struct FCtl {
     int ocnt;
     int dmin;
     int unit;
+    int bad;
+    int ovf;   // a queue push did not fit
 };
 
 // Path counts share a word with the counter, so they are limited to 2^48 - 1 here; a unit
 // that exceeds it stops before its dependency pass and is recomputed by the plain kernel.
 constexpr unsigned long long kSigMax = (1ull << 48) - 1ull;
-enum : int { kErrRetry = 8 };
 
 __device__ __forceinline__ unsigned long long ldcg64(const unsigned long long* p) { return __ldcg(p); }
 __device__ __forceinline__ int dist_of(unsigned long long w) { return (int)(w >> 32); }
 
-// Block-wide push (warp-aggregated slot reservation on a shared-memory counter).
+// Block-wide push (warp-aggregated slot reservation on a shared-memory counter); a push past
+// the capacity is dropped and raises *ovf (the unit is then recomputed elsewhere).
 template <class E>
-__device__ __forceinline__ void bpush(bool want, const E& x, E* q, int* c, int cap, int* err) {
+__device__ __forceinline__ void bpush(bool want, const E& x, E* q, int* c, int cap, int* ovf) {
     const unsigned m = __ballot_sync(kFull, want);
     if (!m) return;
     const int lane = threadIdx.x & 31;
@@ -92,7 +102,7 @@ __device__ __forceinline__ void bpush(bool want, const E& x, E* q, int* c, int c
     if (want) {
         const int pos = base + __popc(m & ((1u << lane) - 1u));
         if (pos < cap) q[pos] = x;
-        else atomicOr(err, kErrQueue);
+        else *ovf = 1;
     }
 }
 
@@ -106,6 +116,7 @@ __device__ void frontier_unit(const KParams& P, int64_t ui, const Unit& u, const
     const int src = u.src;
     const int delta = sg.delta > 0 ? sg.delta : 1;
     const int tid = threadIdx.x, nth = blockDim.x;
+    const int qc_cap = (int)fqcap(cap);
     int bad = 0;
 
     // ---------------------------------------------------------------- distances
@@ -120,6 +131,7 @@ __device__ void frontier_unit(const KParams& P, int64_t ui, const Unit& u, const
         C.ncnt[1] = 0;
         C.fcnt[0] = 0;
         C.fcnt[1] = 0;
+        C.ovf = 0;
     }
     __syncthreads();
     const int64_t capr = (int64_t)P.iter_mult * ((int64_t)n + 2);
@@ -173,13 +185,14 @@ __device__ void frontier_unit(const KParams& P, int64_t ui, const Unit& u, const
                             }
                         }
                         const QEnt qe{x[k], r0[k], r1[k] - r0[k], 0};
-                        bpush(pn, qe, qnx, &C.ncnt[qs ^ 1], cap + 1, P.err);
-                        bpush(pf, qe, qfx, &C.fcnt[fs], cap + 1, P.err);
+                        bpush(pn, qe, qnx, &C.ncnt[qs ^ 1], qc_cap, &C.ovf);
+                        bpush(pf, qe, qfx, &C.fcnt[fs], qc_cap, &C.ovf);
                     }
                     e += 4;
                 }
             }
             __syncthreads();
+            if (C.ovf) { bad = kErrRetry; break; }
             if (tid == 0) C.ncnt[qs] = 0;
             qs ^= 1;
             __syncthreads();
@@ -218,10 +231,11 @@ __device__ void frontier_unit(const KParams& P, int64_t ui, const Unit& u, const
                     S.word[qe.v] = ((unsigned long long)(unsigned)d << 32) | (pn ? nsplit : fst);
                 }
             }
-            bpush(pn, qe, qnx, &C.ncnt[qs], cap + 1, P.err);
-            bpush(pf, qe, qf2, &C.fcnt[fs ^ 1], cap + 1, P.err);
+            bpush(pn, qe, qnx, &C.ncnt[qs], qc_cap, &C.ovf);
+            bpush(pf, qe, qf2, &C.fcnt[fs ^ 1], qc_cap, &C.ovf);
         }
         __syncthreads();
+        if (C.ovf) { bad = kErrRetry; break; }
         if (tid == 0) C.fcnt[fs] = 0;
         fs ^= 1;
         __syncthreads();
@@ -271,7 +285,7 @@ __device__ void frontier_unit(const KParams& P, int64_t ui, const Unit& u, const
         }
         if (tid == 0) {
             const int e0 = __ldg(rp + src);
-            S.order[0] = LEnt{src, 0, e0, __ldg(rp + src + 1) - e0, 1ull, 0u, 0u};
+            S.order[0] = LEnt{src, 0, e0, (unsigned)(__ldg(rp + src + 1) - e0), 1ull};
             S.lvl[0] = 0;
             C.ocnt = 1;
         }
@@ -289,7 +303,7 @@ __device__ void frontier_unit(const KParams& P, int64_t ui, const Unit& u, const
                     dv = o.d;
                     sv = o.sig;
                     e = e0 = o.e0;
-                    e1 = o.e0 + o.deg;
+                    e1 = o.e0 + (int)o.dm;  // still the row length here
                 }
                 while (__any_sync(kFull, e < e1)) {
                     int x[4], nd[4];
@@ -309,7 +323,7 @@ __device__ void frontier_unit(const KParams& P, int64_t ui, const Unit& u, const
 #pragma unroll
                     for (int k = 0; k < 4; ++k) {
                         bool push = false;
-                        LEnt le{x[k], nd[k], 0, 0, 0ull, 0u, 0u};
+                        LEnt le{x[k], nd[k], 0, 0u, 0ull};
                         if (tight[k]) {
                             const int bit = e + k - e0;
                             tmask |= bit < 32 ? (1u << bit) : 0xffffffffu;
@@ -321,13 +335,13 @@ __device__ void frontier_unit(const KParams& P, int64_t ui, const Unit& u, const
                             push = (old & 0xffffull) == 1ull;
                             le.sig = sx;
                             le.e0 = __ldg(rp + x[k]);
-                            le.deg = __ldg(rp + x[k] + 1) - le.e0;
+                            le.dm = (unsigned)(__ldg(rp + x[k] + 1) - le.e0);
                         }
-                        bpush(push, le, S.order, &C.ocnt, cap + 1, P.err);
+                        bpush(push, le, S.order, &C.ocnt, cap + 1, &C.ovf);
                     }
                     e += 4;
                 }
-                if (i < hi) S.order[i].tmask = e1 - e0 > 32 ? 0xffffffffu : tmask;
+                if (i < hi) S.order[i].dm = e1 - e0 > 32 ? 0xffffffffu : tmask;
             }
             __syncthreads();
             ++nlev;
@@ -336,7 +350,12 @@ __device__ void frontier_unit(const KParams& P, int64_t ui, const Unit& u, const
             hi = C.ocnt;
             __syncthreads();
         }
-        bad = __syncthreads_or(bad);
+        // block-wide OR of the status bits (__syncthreads_or would only say "some bit")
+        if (tid == 0) C.bad = 0;
+        __syncthreads();
+        if (bad) atomicOr(&C.bad, bad);
+        __syncthreads();
+        bad = C.bad;
         if (!bad && u.bout >= 0) {
             for (int j = tid; j < sg.nb; j += nth) {
                 const int b = sg.border[j];
@@ -356,9 +375,9 @@ __device__ void frontier_unit(const KParams& P, int64_t ui, const Unit& u, const
                 const int v = o.v, dv = o.d;
                 const unsigned long long sv = o.sig;
                 typename Prec::Acc acc = Prec::zero();
-                if (o.deg <= 32) {
+                if (o.dm != 0xffffffffu) {
                     // tight out-edges only, four at a time (the mask was set by the Kahn pass)
-                    unsigned mk = o.tmask;
+                    unsigned mk = o.dm;
                     while (mk) {
                         int x[4];
 #pragma unroll
@@ -386,7 +405,7 @@ __device__ void frontier_unit(const KParams& P, int64_t ui, const Unit& u, const
                             }
                     }
                 } else {
-                    const int e1 = o.e0 + o.deg;
+                    const int e1 = __ldg(rp + v + 1);
                     for (int e = o.e0; e < e1; ++e) {
                         const int2 a = __ldg(adj + e);
                         if (dv + a.y == dist_of(ldcg64(S.word + a.x))) {
@@ -406,13 +425,8 @@ __device__ void frontier_unit(const KParams& P, int64_t ui, const Unit& u, const
         }
     }
     if (tid == 0 && bad) {
-        if (bad == kErrRetry) {
-            // recomputed on the host's request by the plain kernel (64-bit path counts)
-            const int r = atomicAdd(P.retry_count, 1);
-            if (r < P.retry_cap) P.retry[r] = (int)ui;
-        } else {
-            atomicOr(P.err, bad);
-        }
+        if (bad == kErrRetry) request_retry(P, u, kErrRetry);  // recomputed with 64-bit counts
+        else atomicOr(P.err, bad);
     }
     if (P.dbg_dist) {
         for (int v = tid; v < n; v += nth) {
@@ -431,8 +445,10 @@ __device__ void frontier_unit(const KParams& P, int64_t ui, const Unit& u, const
     __syncthreads();
 }
 
-template <class Prec>
-__global__ void __launch_bounds__(128, 5) frontier_kernel(KParams P) {
+// kWide: 512-thread blocks for segments whose frontiers span many hundreds of vertices
+// (millions of vertices); otherwise 128-thread blocks, five per SM.
+template <class Prec, bool kWide>
+__global__ void __launch_bounds__(kWide ? 512 : 128, kWide ? 1 : 5) frontier_kernel(KParams P) {
     __shared__ FCtl C;
     char* slot = P.ws + (int64_t)blockIdx.x * P.ws_stride;
     unsigned* hdr = (unsigned*)slot;

@@ -335,3 +335,18 @@ def test_grid2048_full_size_sources(fg):
     f64 = fg.dependency_batch(g, src, None, fg.FP64, fg.BATCHED)
     f32 = fg.dependency_batch(g, src, None, fg.FP32C, fg.BATCHED)
     assert rel_err(f32, f64) <= TOL_FP32C
+
+
+def test_large_path_counts_are_recomputed_exactly(fg):
+    """Random geometric graphs with small tied weights have path counts above 2^48 (the batched
+    block kernel's packed field): those units are recomputed by the plain kernel, results equal
+    the FP64 plain path and the oracle."""
+    el = graphs.rgg_knn(51013, seed=7, gid=23)  # the batch's second largest graph
+    og = oracle.CSR.from_edgelist(el)
+    g = fg.Graph.from_edgelist(el)
+    src = np.arange(0, el.n, el.n // 64, dtype=np.int32)[:64]
+    _, sig, _, _ = fg.sssp_debug(g, int(src[0]))
+    a = fg.dependency_batch(g, src, None, fg.FP64, fg.BATCHED)
+    b = fg.dependency_batch(g, src, None, fg.FP64, fg.PLAIN)
+    assert rel_err(a, b) <= TOL_FP64
+    assert rel_err(a, oracle.exact_bc_sources(og, src, threads=8)) <= TOL_FP64
