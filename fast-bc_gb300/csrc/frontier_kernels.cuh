@@ -23,9 +23,10 @@ namespace fbc {
 struct QEnt {
     int v, e0, deg, pad;
 };
-// A vertex of a Kahn level: distance, row start, final path count, and `dm`: the row length
-// until the vertex's own level is processed, then the mask of its tight out-edges, so that the
-// dependency pass reads only those (all ones: re-test every edge of the row).
+// A vertex of a Kahn level: distance, row start, final path count, and `dm`: the mask of its
+// tight out-edges found by the counting sweep (bit k: edge e0 + k), so that the Kahn and
+// dependency passes touch only those; all ones for rows longer than 32 edges (then every edge
+// of the row is re-tested).
 struct LEnt {
     int v, d, e0;
     unsigned dm;
@@ -48,6 +49,7 @@ struct FState {
     QEnt* q[4];                   // near0, near1, far0, far1 (fqcap(cap) entries)
     LEnt* order;                  // cap + 1 entries
     int* lvl;                     // cap + 1 entries
+    unsigned* tmask;              // tight out-edge mask per vertex (cap entries)
 };
 
 template <class Prec>
@@ -55,7 +57,7 @@ __host__ __device__ inline int64_t fstate_bytes(int64_t cap) {
     auto al = [](int64_t x) { return (x + 255) & ~int64_t(255); };
     return al(cap * 8) + al(cap * 8) + al(cap * (int64_t)sizeof(typename Prec::D)) +
            4 * al(fqcap(cap) * (int64_t)sizeof(QEnt)) + al((cap + 1) * (int64_t)sizeof(LEnt)) +
-           al((cap + 1) * 4);
+           al((cap + 1) * 4) + al(cap * 4);
 }
 
 template <class Prec>
@@ -67,7 +69,8 @@ __device__ inline FState<Prec> fstate_carve(char* p, int64_t cap) {
     s.dlt = (typename Prec::D*)p; p += al(cap * (int64_t)sizeof(typename Prec::D));
     for (int i = 0; i < 4; ++i) { s.q[i] = (QEnt*)p; p += al(fqcap(cap) * (int64_t)sizeof(QEnt)); }
     s.order = (LEnt*)p; p += al((cap + 1) * (int64_t)sizeof(LEnt));
-    s.lvl = (int*)p;
+    s.lvl = (int*)p; p += al((cap + 1) * 4);
+    s.tmask = (unsigned*)p;
     return s;
 }
 
@@ -245,18 +248,21 @@ __device__ void frontier_unit(const KParams& P, int64_t ui, const Unit& u, const
     int nlev = 0;
     if (!bad) {
         // ------------------------------------------------------------- sigma (Kahn)
-        // tight in-edge counts: a sweep over all vertices, four per thread in flight
+        // tight in-edge counts and each vertex's tight out-edge mask: a sweep over all
+        // vertices, four per thread in flight
         for (int v0 = tid; v0 < n; v0 += 4 * nth) {
-            int dv[4], e[4], e1[4];
+            int dv[4], e[4], e1[4], eb[4];
+            unsigned mk[4];
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
                 const int v = v0 + k * nth;
                 dv[k] = kInf;
-                e[k] = e1[k] = 0;
+                e[k] = e1[k] = eb[k] = 0;
+                mk[k] = 0u;
                 if (v < n) {
                     dv[k] = dist_of(ldcg64(S.word + v));
                     if (dv[k] != kInf) {
-                        e[k] = __ldg(rp + v);
+                        e[k] = eb[k] = __ldg(rp + v);
                         e1[k] = __ldg(rp + v + 1);
                     }
                 }
@@ -280,12 +286,22 @@ __device__ void frontier_unit(const KParams& P, int64_t ui, const Unit& u, const
                 for (int k = 0; k < 4; ++k) dx[k] = x[k] >= 0 ? dist_of(ldcg64(S.word + x[k])) : -1;
 #pragma unroll
                 for (int k = 0; k < 4; ++k)
-                    if (x[k] >= 0 && nd[k] == dx[k]) atomicAdd(S.sc + x[k], 1ull);
+                    if (x[k] >= 0 && nd[k] == dx[k]) {
+                        atomicAdd(S.sc + x[k], 1ull);
+                        const int bit = e[k] - 1 - eb[k];
+                        if (bit < 32) mk[k] |= 1u << bit;
+                    }
+            }
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const int v = v0 + k * nth;
+                if (v < n && dv[k] != kInf) S.tmask[v] = e1[k] - eb[k] > 32 ? 0xffffffffu : mk[k];
             }
         }
+        __syncthreads();
         if (tid == 0) {
             const int e0 = __ldg(rp + src);
-            S.order[0] = LEnt{src, 0, e0, (unsigned)(__ldg(rp + src + 1) - e0), 1ull};
+            S.order[0] = LEnt{src, 0, e0, __ldcg(S.tmask + src), 1ull};
             S.lvl[0] = 0;
             C.ocnt = 1;
         }
@@ -295,38 +311,50 @@ __device__ void frontier_unit(const KParams& P, int64_t ui, const Unit& u, const
             if (nlev >= n) { bad = kErrIter; break; }
             for (int base = lo + (tid & ~31); base < hi; base += nth) {
                 const int i = base + (tid & 31);
-                int e = 0, e1 = 0, dv = 0, e0 = 0;
+                int dv = 0, e0 = 0, e = 0, e1 = 0;
+                unsigned mk = 0u;
                 unsigned long long sv = 0;
-                unsigned tmask = 0u;
                 if (i < hi) {
                     const LEnt o = S.order[i];
                     dv = o.d;
                     sv = o.sig;
-                    e = e0 = o.e0;
-                    e1 = o.e0 + (int)o.dm;  // still the row length here
+                    e0 = o.e0;
+                    mk = o.dm;
+                    if (mk == 0xffffffffu) {  // long row: walk it and re-test every edge
+                        e = e0;
+                        e1 = __ldg(rp + o.v + 1);
+                        mk = 0u;
+                    }
                 }
-                while (__any_sync(kFull, e < e1)) {
+                while (__any_sync(kFull, mk != 0u || e < e1)) {
                     int x[4], nd[4];
+                    bool tight[4];
 #pragma unroll
                     for (int k = 0; k < 4; ++k) {
                         x[k] = -1;
-                        if (e + k < e1) {
-                            const int2 a = __ldg(adj + e + k);
+                        tight[k] = false;
+                        int ei = -1;
+                        if (mk) {  // tight by the counting sweep
+                            ei = e0 + __ffs(mk) - 1;
+                            mk &= mk - 1u;
+                            tight[k] = true;
+                        } else if (e < e1) {
+                            ei = e++;
+                        }
+                        if (ei >= 0) {
+                            const int2 a = __ldg(adj + ei);
                             x[k] = a.x;
                             nd[k] = dv + a.y;
                         }
                     }
-                    bool tight[4];
 #pragma unroll
                     for (int k = 0; k < 4; ++k)
-                        tight[k] = x[k] >= 0 && nd[k] == dist_of(ldcg64(S.word + x[k]));
+                        if (x[k] >= 0 && !tight[k]) tight[k] = nd[k] == dist_of(ldcg64(S.word + x[k]));
 #pragma unroll
                     for (int k = 0; k < 4; ++k) {
                         bool push = false;
                         LEnt le{x[k], nd[k], 0, 0u, 0ull};
                         if (tight[k]) {
-                            const int bit = e + k - e0;
-                            tmask |= bit < 32 ? (1u << bit) : 0xffffffffu;
                             // one atomic adds sigma_v and retires the edge; the thread that
                             // retires the last tight in-edge knows x's final count
                             const unsigned long long old = atomicAdd(S.sc + x[k], (sv << 16) - 1ull);
@@ -334,14 +362,12 @@ __device__ void frontier_unit(const KParams& P, int64_t ui, const Unit& u, const
                             if (sx > kSigMax || sv > kSigMax) bad |= kErrRetry;
                             push = (old & 0xffffull) == 1ull;
                             le.sig = sx;
-                            le.e0 = __ldg(rp + x[k]);
-                            le.dm = (unsigned)(__ldg(rp + x[k] + 1) - le.e0);
+                            le.e0 = __ldg(rp + x[k]);        // in flight with the atomic
+                            le.dm = __ldcg(S.tmask + x[k]);
                         }
                         bpush(push, le, S.order, &C.ocnt, cap + 1, &C.ovf);
                     }
-                    e += 4;
                 }
-                if (i < hi) S.order[i].dm = e1 - e0 > 32 ? 0xffffffffu : tmask;
             }
             __syncthreads();
             ++nlev;
