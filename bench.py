@@ -519,7 +519,7 @@ def main():
     if dist:
         dist.barrier()
     clocks = Clocks(local) if rank == 0 else None
-    dev_ms, wall_ms, h2d, d2h, launches = [], [], 0, 0, 0
+    dev_ms, wall_ms, sweep_wall, h2d, d2h, launches = [], [], [], 0, 0, 0
     kern = {"warp_ms": 0.0, "block_ms": 0.0, "warp_bytes": 0.0, "block_bytes": 0.0}
     for _ in range(args.steps):
         flush.zero_()
@@ -527,6 +527,7 @@ def main():
         t0 = time.perf_counter()
         bc, st1, st2 = step()
         wall_ms.append((time.perf_counter() - t0) * 1e3)
+        sweep_wall.append(st1.wall_ms)
         dev_ms.append(st1.kernel_ms + st2.kernel_ms)
         h2d += st1.h2d_bytes + st2.h2d_bytes
         d2h += st1.d2h_bytes + st2.d2h_bytes
@@ -535,6 +536,27 @@ def main():
             kern[k] += getattr(st1, k) + getattr(st2, k)
     torch.cuda.synchronize()
     clk = clocks.stop() if clocks else None
+    sweep = None
+    if sched == fg.BATCHED:
+        # the cluster sweep once more, as a prepared plan replayed from a captured CUDA graph
+        # (outside the timed steps above; compared with the per-call sweep's wall time)
+        knobs("clusters")
+        plan = fg.ClusterPlan(g, cs, prec)
+        for _ in range(2):
+            plan.run()
+        rw, rd = [], []
+        for _ in range(max(args.steps, 1)):
+            flush.zero_()
+            torch.cuda.synchronize()
+            st = fg.Stats()
+            t0 = time.perf_counter()
+            plan.run(st, copy=False)
+            rw.append((time.perf_counter() - t0) * 1e3)
+            rd.append(st.kernel_ms)
+        sweep = {"captured": plan.captured, "replay_wall_ms": float(np.median(rw)),
+                 "replay_device_ms": float(np.median(rd)),
+                 "per_call_wall_ms": float(np.median(sweep_wall)) if sweep_wall else None}
+        plan.free()
     tot_dev = sum(dev_ms) / 1e3
     tot_wall = sum(wall_ms) / 1e3
     if dist:
@@ -575,6 +597,7 @@ def main():
             "e2e": {"value": e2e, "unit": "GTEPS", "h2d_bytes_per_step": h2d // args.steps,
                     "d2h_bytes_per_step": d2h // args.steps, "s_per_graph": tot_wall / args.steps},
             "gpu_launches": launches,
+            "cluster_sweep": sweep,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "kernel": dom,
                          "peak_source": peak_src,

@@ -8,6 +8,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <memory>
 #include <mutex>
 #include <numeric>
 #include <string>
@@ -129,6 +130,24 @@ struct fbc_graph_s {
     std::vector<int64_t> h_rp;
     std::vector<int32_t> h_col;
     std::vector<int32_t> h_w;
+};
+
+struct fbc_plan_s {
+    fbc_graph_s* G = nullptr;
+    int prec = FBC_PREC_FP32C;
+    int64_t n = 0, ent = 0;
+    DBuf crp, cadj, cgid, cbord, segs, units, chunks, bc, bdist, bsig, ctr, retry;
+    double* h_bc = nullptr;
+    double* h_bdist = nullptr;
+    uint64_t* h_bsig = nullptr;
+    int* h_ctl = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    bool captured = false;
+    double relax = 0, bytes = 0;
+    int64_t nunits = 0;
+    std::vector<int64_t> coff, boff;
+    std::vector<int32_t> cverts, borders;
 };
 
 namespace {
@@ -334,52 +353,72 @@ bool small_fits(int nmax, int mmax, int warps) {
     return L.pool + warps * fbc::SmallLayout::per_warp(nmax) <= small_dyn_smem();
 }
 
+// Host side of a small-segment launch: warps per block, dynamic shared memory, the
+// (segment, chunk) work items (units grouped by segment, biggest segments first) and the grid.
+struct SmallCfg {
+    int wpb = 0;
+    int64_t dyn = 0;
+    int64_t blocks = 0;
+    std::vector<fbc::Chunk> chunks;
+};
+
+int small_config(const Plan& P, const std::vector<Unit>& units, int nmax, int mmax, int nmin, SmallCfg& c) {
+    const fbc::SmallLayout L(nmax, mmax);
+    c.dyn = small_dyn_smem();
+    if (!small_fits(nmax, mmax, 1)) return fail(FBC_ERR_INVALID_ARG, "small-segment kernel does not fit");
+    c.wpb = (int)std::max<int64_t>(
+        1, std::min<int64_t>(16, (c.dyn - L.pool) / fbc::SmallLayout::per_warp(std::max(nmin, 1))));
+    // large chunks keep the block's warps busy between the barriers that reload the CSR;
+    // about two chunks per block still balance the blocks
+    const int64_t per_chunk = std::max<int64_t>(
+        4 * c.wpb, std::min<int64_t>(g.opt.chunk_max, (int64_t)units.size() / std::max<int64_t>(1, (int64_t)g.nsm * 2)));
+    c.chunks.clear();
+    for (size_t i = 0; i < units.size();) {
+        size_t j = i;
+        while (j < units.size() && units[j].seg == units[i].seg && (int64_t)(j - i) < per_chunk) ++j;
+        c.chunks.push_back(fbc::Chunk{units[i].seg, (int32_t)i, (int32_t)(j - i), 0});
+        i = j;
+    }
+    std::stable_sort(c.chunks.begin(), c.chunks.end(), [&](const fbc::Chunk& a, const fbc::Chunk& b) {
+        return P.segs[a.seg].n > P.segs[b.seg].n;
+    });
+    c.blocks = std::min<int64_t>((int64_t)g.nsm, (int64_t)c.chunks.size());
+    return FBC_OK;
+}
+
+template <class Prec>
+int small_launch(const SmallCfg& c, const fbc::SmallParams& S) {
+    auto kern = fbc::small_seg_kernel<Prec>;
+    FBC_CK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c.dyn));
+    kern<<<(unsigned)c.blocks, 32 * c.wpb, (size_t)c.dyn, g.st>>>(S);
+    FBC_CK(cudaGetLastError());
+    return FBC_OK;
+}
+
 template <class Prec>
 int launch_small(const Plan& P, const std::vector<Unit>& units, int nmax, int mmax, int nmin,
                  fbc_stats* st, int& launches) {
     if (units.empty()) return FBC_OK;
-    const fbc::SmallLayout L(nmax, mmax);
-    const int64_t dyn = small_dyn_smem();
-    if (!small_fits(nmax, mmax, 1)) return fail(FBC_ERR_INVALID_ARG, "small-segment kernel does not fit");
-    const int wpb = (int)std::max<int64_t>(
-        1, std::min<int64_t>(16, (dyn - L.pool) / fbc::SmallLayout::per_warp(std::max(nmin, 1))));
-    // chunks: consecutive units of one segment, enough of them to balance the SMs
-    std::vector<fbc::Chunk> ch;
-    // large chunks keep the block's warps busy between the barriers that reload the CSR;
-    // about two chunks per block still balance the blocks
-    const int64_t per_chunk = std::max<int64_t>(
-        4 * wpb, std::min<int64_t>(g.opt.chunk_max, (int64_t)units.size() / std::max<int64_t>(1, (int64_t)g.nsm * 2)));
-    for (size_t i = 0; i < units.size();) {
-        size_t j = i;
-        while (j < units.size() && units[j].seg == units[i].seg && (int64_t)(j - i) < per_chunk) ++j;
-        ch.push_back(fbc::Chunk{units[i].seg, (int32_t)i, (int32_t)(j - i), 0});
-        i = j;
-    }
-    std::stable_sort(ch.begin(), ch.end(), [&](const fbc::Chunk& a, const fbc::Chunk& b) {
-        return P.segs[a.seg].n > P.segs[b.seg].n;
-    });
+    SmallCfg c;
+    FBC_TRY(small_config(P, units, nmax, mmax, nmin, c));
     FBC_CK(g.units_w.ensure(sizeof(Unit) * units.size()));
     FBC_CK(cudaMemcpyAsync(g.units_w.p, units.data(), sizeof(Unit) * units.size(),
                            cudaMemcpyHostToDevice, g.st));
-    FBC_CK(g.chunks.ensure(sizeof(fbc::Chunk) * ch.size()));
-    FBC_CK(cudaMemcpyAsync(g.chunks.p, ch.data(), sizeof(fbc::Chunk) * ch.size(),
+    FBC_CK(g.chunks.ensure(sizeof(fbc::Chunk) * c.chunks.size()));
+    FBC_CK(cudaMemcpyAsync(g.chunks.p, c.chunks.data(), sizeof(fbc::Chunk) * c.chunks.size(),
                            cudaMemcpyHostToDevice, g.st));
-    if (st) st->h2d_bytes += (int64_t)(sizeof(Unit) * units.size() + sizeof(fbc::Chunk) * ch.size());
+    if (st) st->h2d_bytes += (int64_t)(sizeof(Unit) * units.size() + sizeof(fbc::Chunk) * c.chunks.size());
     fbc::SmallParams S{};
     S.k = base_params(P);
     S.k.units = g.units_w.as<Unit>();
     S.k.nunits = (int64_t)units.size();
     S.chunks = g.chunks.as<fbc::Chunk>();
-    S.nchunks = (int32_t)ch.size();
+    S.nchunks = (int32_t)c.chunks.size();
     S.nmax = nmax;
     S.mmax = mmax;
-    S.smem = (int32_t)dyn;
+    S.smem = (int32_t)c.dyn;
     S.next_chunk = g.ctr.as<unsigned long long>() + 1;
-    auto kern = fbc::small_seg_kernel<Prec>;
-    FBC_CK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
-    const int64_t blocks = std::min<int64_t>((int64_t)g.nsm, (int64_t)ch.size());
-    kern<<<(unsigned)blocks, 32 * wpb, (size_t)dyn, g.st>>>(S);
-    FBC_CK(cudaGetLastError());
+    FBC_TRY(small_launch<Prec>(c, S));
     ++launches;
     return FBC_OK;
 }
@@ -579,6 +618,99 @@ int cluster_ids(const fbc_graph_s* G, int32_t nclusters, const int64_t* coff, co
             cid[v] = c;
         }
     }
+    return FBC_OK;
+}
+
+// Host side of a batched cluster evaluation: cluster ids, borders (computed when not given),
+// the induced-subgraph CSR of every cluster with local ids (SubGraph::forwardStar keeps the
+// intra-cluster edges), uploaded into the given device buffers, and the plan's segments and
+// units (border-output row of the i-th vertex of cluster c: E_c + i * nb_c).
+int prepare_clusters(const fbc_graph_s* G, int32_t nclusters, const int64_t* coff, const int32_t* cverts,
+                     const int64_t* border_off, const int32_t* borders, int precision, int sched,
+                     DBuf& crp, DBuf& cadj, DBuf& cgid, DBuf& cbord, Plan& P, int64_t& ent, fbc_stats* st) {
+    std::vector<int32_t> cid;
+    FBC_TRY(cluster_ids(G, nclusters, coff, cverts, cid));
+    std::vector<int64_t> boff_v;
+    std::vector<int32_t> bl_v;
+    if (!border_off) {
+        compute_borders(G, nclusters, coff, cverts, cid, boff_v, bl_v);
+        border_off = boff_v.data();
+        borders = bl_v.data();
+    }
+    std::vector<int32_t> lid((size_t)G->n, -1);
+    for (int32_t c = 0; c < nclusters; ++c)
+        for (int64_t i = coff[c]; i < coff[c + 1]; ++i) lid[cverts[i]] = (int32_t)(i - coff[c]);
+    const int64_t nv = coff[nclusters];
+    std::vector<int32_t> hrp;
+    std::vector<int2> hadj;
+    std::vector<int32_t> hbord;
+    std::vector<int64_t> rp_off((size_t)nclusters), adj_off((size_t)nclusters), b_off((size_t)nclusters);
+    std::vector<int64_t> seg_m((size_t)nclusters);
+    hrp.reserve((size_t)(nv + nclusters));
+    for (int32_t c = 0; c < nclusters; ++c) {
+        rp_off[c] = (int64_t)hrp.size();
+        adj_off[c] = (int64_t)hadj.size();
+        int32_t e = 0;
+        hrp.push_back(0);
+        for (int64_t i = coff[c]; i < coff[c + 1]; ++i) {
+            const int32_t v = cverts[i];
+            for (int64_t k = G->h_rp[v]; k < G->h_rp[v + 1]; ++k) {
+                const int32_t x = G->h_col[k];
+                if (cid[x] == c) {
+                    hadj.push_back(make_int2(lid[x], G->h_w[k]));
+                    ++e;
+                }
+            }
+            hrp.push_back(e);
+        }
+        seg_m[c] = e;
+        b_off[c] = (int64_t)hbord.size();
+        for (int64_t j = border_off[c]; j < border_off[c + 1]; ++j) {
+            const int32_t b = borders[j];
+            if (b < 0 || b >= G->n || cid[b] != c)
+                return fail(FBC_ERR_INVALID_ARG, "border vertex not in its cluster");
+            hbord.push_back(lid[b]);
+        }
+    }
+    FBC_CK(crp.ensure(sizeof(int32_t) * std::max<size_t>(hrp.size(), 1)));
+    FBC_CK(cadj.ensure(sizeof(int2) * std::max<size_t>(hadj.size(), 1)));
+    FBC_CK(cgid.ensure(sizeof(int32_t) * std::max<int64_t>(nv, 1)));
+    FBC_CK(cbord.ensure(sizeof(int32_t) * std::max<size_t>(hbord.size(), 1)));
+    if (!hrp.empty())
+        FBC_CK(cudaMemcpyAsync(crp.p, hrp.data(), sizeof(int32_t) * hrp.size(), cudaMemcpyHostToDevice, g.st));
+    if (!hadj.empty())
+        FBC_CK(cudaMemcpyAsync(cadj.p, hadj.data(), sizeof(int2) * hadj.size(), cudaMemcpyHostToDevice, g.st));
+    if (nv > 0)
+        FBC_CK(cudaMemcpyAsync(cgid.p, cverts, sizeof(int32_t) * (size_t)nv, cudaMemcpyHostToDevice, g.st));
+    if (!hbord.empty())
+        FBC_CK(cudaMemcpyAsync(cbord.p, hbord.data(), sizeof(int32_t) * hbord.size(), cudaMemcpyHostToDevice, g.st));
+    FBC_CK(cudaStreamSynchronize(g.st));  // the host vectors go out of scope
+    if (st)
+        st->h2d_bytes += (int64_t)(sizeof(int32_t) * (hrp.size() + (size_t)nv + hbord.size()) +
+                                   sizeof(int2) * hadj.size());
+    P.prec = precision;
+    P.sched = sched;
+    ent = 0;
+    const int dl = delta_for(G->meanw);
+    for (int32_t c = 0; c < nclusters; ++c) {
+        Seg s{};
+        s.rp = crp.as<int32_t>() + rp_off[c];
+        s.adj = cadj.as<int2>() + adj_off[c];
+        s.gid = cgid.as<int32_t>() + coff[c];
+        s.border = cbord.as<int32_t>() + b_off[c];
+        s.out_base = 0;
+        s.n = (int32_t)(coff[c + 1] - coff[c]);
+        s.nb = (int32_t)(border_off[c + 1] - border_off[c]);
+        s.delta = dl;
+        P.segs.push_back(s);
+        P.seg_m.push_back(seg_m[c]);
+        P.seg_maxw.push_back(G->maxw);
+        P.seg_maxindeg.push_back(G->maxindeg);
+        for (int32_t i = 0; i < s.n; ++i) P.units.push_back(Unit{c, i, 1.0, ent + (int64_t)i * s.nb});
+        ent += (int64_t)s.n * s.nb;
+    }
+    P.bc_len = G->n;
+    P.border_entries = ent;
     return FBC_OK;
 }
 
@@ -861,91 +993,10 @@ int fbc_cluster_eval_batch(fbc_graph G, int32_t nclusters, const int64_t* coff,
     if (border_off && !borders) return fail(FBC_ERR_INVALID_ARG, "border_off without borders");
     const double t0 = now_ms();
     if (st) std::memset(st, 0, sizeof(*st));
-    std::vector<int32_t> cid;
-    FBC_TRY(cluster_ids(G, nclusters, coff, cverts, cid));
-    std::vector<int64_t> boff_v;
-    std::vector<int32_t> bl_v;
-    if (!border_off) {
-        compute_borders(G, nclusters, coff, cverts, cid, boff_v, bl_v);
-        border_off = boff_v.data();
-        borders = bl_v.data();
-    }
-    // local ids: position of each vertex in its cluster's list
-    std::vector<int32_t> lid((size_t)G->n, -1);
-    for (int32_t c = 0; c < nclusters; ++c)
-        for (int64_t i = coff[c]; i < coff[c + 1]; ++i) lid[cverts[i]] = (int32_t)(i - coff[c]);
-    // induced-subgraph CSRs (SubGraph::forwardStar keeps the intra-cluster edges)
-    const int64_t nv = coff[nclusters];
-    std::vector<int32_t> hrp;
-    std::vector<int2> hadj;
-    std::vector<int32_t> hbord;
-    std::vector<int64_t> rp_off((size_t)nclusters), adj_off((size_t)nclusters), b_off((size_t)nclusters);
-    std::vector<int64_t> seg_m((size_t)nclusters);
-    hrp.reserve((size_t)(nv + nclusters));
-    for (int32_t c = 0; c < nclusters; ++c) {
-        rp_off[c] = (int64_t)hrp.size();
-        adj_off[c] = (int64_t)hadj.size();
-        int32_t e = 0;
-        hrp.push_back(0);
-        for (int64_t i = coff[c]; i < coff[c + 1]; ++i) {
-            const int32_t v = cverts[i];
-            for (int64_t k = G->h_rp[v]; k < G->h_rp[v + 1]; ++k) {
-                const int32_t x = G->h_col[k];
-                if (cid[x] == c) {
-                    hadj.push_back(make_int2(lid[x], G->h_w[k]));
-                    ++e;
-                }
-            }
-            hrp.push_back(e);
-        }
-        seg_m[c] = e;
-        b_off[c] = (int64_t)hbord.size();
-        for (int64_t j = border_off[c]; j < border_off[c + 1]; ++j) {
-            const int32_t b = borders[j];
-            if (b < 0 || b >= G->n || cid[b] != c)
-                return fail(FBC_ERR_INVALID_ARG, "border vertex not in its cluster");
-            hbord.push_back(lid[b]);
-        }
-    }
-    FBC_CK(g.crp.ensure(sizeof(int32_t) * std::max<size_t>(hrp.size(), 1)));
-    FBC_CK(g.cadj.ensure(sizeof(int2) * std::max<size_t>(hadj.size(), 1)));
-    FBC_CK(g.cgid.ensure(sizeof(int32_t) * std::max<int64_t>(nv, 1)));
-    FBC_CK(g.cbord.ensure(sizeof(int32_t) * std::max<size_t>(hbord.size(), 1)));
-    if (!hrp.empty())
-        FBC_CK(cudaMemcpyAsync(g.crp.p, hrp.data(), sizeof(int32_t) * hrp.size(), cudaMemcpyHostToDevice, g.st));
-    if (!hadj.empty())
-        FBC_CK(cudaMemcpyAsync(g.cadj.p, hadj.data(), sizeof(int2) * hadj.size(), cudaMemcpyHostToDevice, g.st));
-    if (nv > 0)
-        FBC_CK(cudaMemcpyAsync(g.cgid.p, cverts, sizeof(int32_t) * (size_t)nv, cudaMemcpyHostToDevice, g.st));
-    if (!hbord.empty())
-        FBC_CK(cudaMemcpyAsync(g.cbord.p, hbord.data(), sizeof(int32_t) * hbord.size(), cudaMemcpyHostToDevice, g.st));
-    if (st)
-        st->h2d_bytes += (int64_t)(sizeof(int32_t) * (hrp.size() + (size_t)nv + hbord.size()) +
-                                   sizeof(int2) * hadj.size());
     Plan P;
-    P.prec = precision;
-    P.sched = sched;
     int64_t ent = 0;
-    const int dl = delta_for(G->meanw);
-    for (int32_t c = 0; c < nclusters; ++c) {
-        Seg s{};
-        s.rp = g.crp.as<int32_t>() + rp_off[c];
-        s.adj = g.cadj.as<int2>() + adj_off[c];
-        s.gid = g.cgid.as<int32_t>() + coff[c];
-        s.border = g.cbord.as<int32_t>() + b_off[c];
-        s.out_base = 0;
-        s.n = (int32_t)(coff[c + 1] - coff[c]);
-        s.nb = (int32_t)(border_off[c + 1] - border_off[c]);
-        s.delta = dl;
-        P.segs.push_back(s);
-        P.seg_m.push_back(seg_m[c]);
-        P.seg_maxw.push_back(G->maxw);
-    P.seg_maxindeg.push_back(G->maxindeg);
-        for (int32_t i = 0; i < s.n; ++i) P.units.push_back(Unit{c, i, 1.0, ent + (int64_t)i * s.nb});
-        ent += (int64_t)s.n * s.nb;
-    }
-    P.bc_len = G->n;
-    P.border_entries = ent;
+    FBC_TRY(prepare_clusters(G, nclusters, coff, cverts, border_off, borders, precision, sched,
+                             g.crp, g.cadj, g.cgid, g.cbord, P, ent, st));
     FBC_TRY(run_plan(P, st));
     FBC_TRY(download_bc(out_intra_bc, G->n, true, st));
     if (ent > 0 && (out_bdist || out_bsig)) {
@@ -957,6 +1008,169 @@ int fbc_cluster_eval_batch(fbc_graph G, int32_t nclusters, const int64_t* coff,
         if (st) st->d2h_bytes += ent * (int64_t)((out_bdist ? 8 : 0) + (out_bsig ? 8 : 0));
     }
     if (st) st->wall_ms = now_ms() - t0;
+    return FBC_OK;
+}
+
+int fbc_cluster_plan_create(fbc_graph G, int32_t nclusters, const int64_t* coff, const int32_t* cverts,
+                            const int64_t* border_off, const int32_t* borders, int precision,
+                            fbc_plan* out) {
+    std::lock_guard<std::recursive_mutex> lk(g_mu);
+    FBC_TRY(check_init());
+    if (!G || !out || nclusters < 0 || !coff) return fail(FBC_ERR_INVALID_ARG, "null argument");
+    if (precision != FBC_PREC_FP64 && precision != FBC_PREC_FP32C) return fail(FBC_ERR_INVALID_ARG, "unknown precision");
+    *out = nullptr;
+    auto* p = new fbc_plan_s();
+    std::unique_ptr<fbc_plan_s> guard(p);
+    p->G = G;
+    p->prec = precision;
+    p->n = G->n;
+    p->coff.assign(coff, coff + nclusters + 1);
+    p->cverts.assign(cverts, cverts + coff[nclusters]);
+    if (border_off) {
+        p->boff.assign(border_off, border_off + nclusters + 1);
+        p->borders.assign(borders, borders + border_off[nclusters]);
+    }
+    Plan P;
+    FBC_TRY(prepare_clusters(G, nclusters, coff, cverts, border_off, borders, precision, FBC_SCHED_BATCHED,
+                             p->crp, p->cadj, p->cgid, p->cbord, P, p->ent, nullptr));
+    int nmax = 0, mmax = 0, nmin = 1 << 30;
+    bool small = true;
+    for (size_t k = 0; k < P.segs.size(); ++k) {
+        small = small && P.segs[k].n <= std::min<int64_t>(g.opt.warp_max_n, 65535) && P.seg_maxw[k] < 65536;
+        nmax = std::max(nmax, P.segs[k].n);
+        mmax = std::max<int>(mmax, (int)P.seg_m[k]);
+        if (P.segs[k].n > 0) nmin = std::min(nmin, P.segs[k].n);
+    }
+    small = small && !P.units.empty() && small_fits(nmax, mmax, 2);
+    for (const Unit& u : P.units) {
+        p->relax += (double)P.seg_m[u.seg];
+        p->bytes += 40.0 * (double)P.seg_m[u.seg] + 52.0 * P.segs[u.seg].n;
+    }
+    p->nunits = (int64_t)P.units.size();
+    const size_t n8 = sizeof(double) * (size_t)std::max<int64_t>(p->n, 1);
+    const size_t e8 = 8 * (size_t)std::max<int64_t>(p->ent, 1);
+    FBC_CK(cudaMallocHost(&p->h_bc, n8));
+    FBC_CK(cudaMallocHost(&p->h_bdist, e8));
+    FBC_CK(cudaMallocHost(&p->h_bsig, e8));
+    FBC_CK(cudaMallocHost(&p->h_ctl, 64));
+    if (small) {
+        SmallCfg cfg;
+        FBC_TRY(small_config(P, P.units, nmax, mmax, nmin, cfg));
+        FBC_CK(p->segs.ensure(sizeof(Seg) * P.segs.size()));
+        FBC_CK(p->units.ensure(sizeof(Unit) * P.units.size()));
+        FBC_CK(p->chunks.ensure(sizeof(fbc::Chunk) * cfg.chunks.size()));
+        FBC_CK(p->bc.ensure(n8));
+        FBC_CK(p->bdist.ensure(e8));
+        FBC_CK(p->bsig.ensure(e8));
+        FBC_CK(p->ctr.ensure(64));
+        FBC_CK(p->retry.ensure(sizeof(fbc::RetryRec) * P.units.size()));
+        FBC_CK(cudaMemcpyAsync(p->segs.p, P.segs.data(), sizeof(Seg) * P.segs.size(), cudaMemcpyHostToDevice, g.st));
+        FBC_CK(cudaMemcpyAsync(p->units.p, P.units.data(), sizeof(Unit) * P.units.size(), cudaMemcpyHostToDevice, g.st));
+        FBC_CK(cudaMemcpyAsync(p->chunks.p, cfg.chunks.data(), sizeof(fbc::Chunk) * cfg.chunks.size(),
+                               cudaMemcpyHostToDevice, g.st));
+        FBC_CK(cudaStreamSynchronize(g.st));
+        fbc::SmallParams S{};
+        S.k.segs = p->segs.as<Seg>();
+        S.k.units = p->units.as<Unit>();
+        S.k.nunits = (int64_t)P.units.size();
+        S.k.bc = p->bc.as<double>();
+        S.k.bdist = p->bdist.as<double>();
+        S.k.bsig = p->bsig.as<unsigned long long>();
+        S.k.err = (int*)(p->ctr.as<unsigned long long>() + 2);
+        S.k.retry_count = S.k.err + 1;
+        S.k.retry = p->retry.as<fbc::RetryRec>();
+        S.k.retry_cap = (int32_t)P.units.size();
+        S.k.iter_mult = (int32_t)g.opt.iter_mult;
+        S.chunks = p->chunks.as<fbc::Chunk>();
+        S.nchunks = (int32_t)cfg.chunks.size();
+        S.nmax = nmax;
+        S.mmax = mmax;
+        S.smem = (int32_t)cfg.dyn;
+        S.next_chunk = p->ctr.as<unsigned long long>() + 1;
+        const bool f64 = precision == FBC_PREC_FP64;
+        if (f64) FBC_CK(cudaFuncSetAttribute(fbc::small_seg_kernel<fbc::PrecF64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cfg.dyn));
+        else FBC_CK(cudaFuncSetAttribute(fbc::small_seg_kernel<fbc::PrecDF32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cfg.dyn));
+        // capture: reset counters and the BC accumulator, run the sweep, download into pinned memory
+        FBC_CK(cudaStreamBeginCapture(g.st, cudaStreamCaptureModeThreadLocal));
+        cudaMemsetAsync(p->ctr.p, 0, 64, g.st);
+        cudaMemsetAsync(p->bc.p, 0, n8, g.st);
+        if (f64) fbc::small_seg_kernel<fbc::PrecF64><<<(unsigned)cfg.blocks, 32 * cfg.wpb, (size_t)cfg.dyn, g.st>>>(S);
+        else fbc::small_seg_kernel<fbc::PrecDF32><<<(unsigned)cfg.blocks, 32 * cfg.wpb, (size_t)cfg.dyn, g.st>>>(S);
+        cudaMemcpyAsync(p->h_bc, p->bc.p, n8, cudaMemcpyDeviceToHost, g.st);
+        if (p->ent > 0) {
+            cudaMemcpyAsync(p->h_bdist, p->bdist.p, e8, cudaMemcpyDeviceToHost, g.st);
+            cudaMemcpyAsync(p->h_bsig, p->bsig.p, e8, cudaMemcpyDeviceToHost, g.st);
+        }
+        cudaMemcpyAsync(p->h_ctl, (char*)p->ctr.p + 16, 8, cudaMemcpyDeviceToHost, g.st);
+        FBC_CK(cudaStreamEndCapture(g.st, &p->graph));
+        FBC_CK(cudaGraphInstantiate(&p->exec, p->graph, 0));
+        p->captured = true;
+    }
+    *out = guard.release();
+    return FBC_OK;
+}
+
+int fbc_plan_run(fbc_plan p, fbc_stats* st) {
+    std::lock_guard<std::recursive_mutex> lk(g_mu);
+    FBC_TRY(check_init());
+    if (!p) return fail(FBC_ERR_INVALID_ARG, "null plan");
+    const double t0 = now_ms();
+    if (st) std::memset(st, 0, sizeof(*st));
+    if (p->captured) {
+        FBC_CK(cudaEventRecord(g.ev0, g.st));
+        FBC_CK(cudaGraphLaunch(p->exec, g.st));
+        FBC_CK(cudaEventRecord(g.ev1, g.st));
+        FBC_CK(cudaStreamSynchronize(g.st));
+        if (p->h_ctl[0] == 0 && p->h_ctl[1] == 0) {
+            if (st) {
+                float ms = 0.f;
+                FBC_CK(cudaEventElapsedTime(&ms, g.ev0, g.ev1));
+                st->kernel_ms = ms;
+                st->warp_ms = ms;
+                st->units = st->warp_units = p->nunits;
+                st->relaxations = p->relax;
+                st->warp_bytes = p->bytes;
+                st->launches = 1;
+                st->d2h_bytes = 8 * (p->n + 2 * p->ent);
+                st->wall_ms = now_ms() - t0;
+            }
+            return FBC_OK;
+        }
+        if (p->h_ctl[0] != 0 && p->h_ctl[1] == 0) return map_err(p->h_ctl[0]);
+    }
+    // not captured, or path counts needed a wider representation: the general path
+    std::memset(p->h_bc, 0, sizeof(double) * (size_t)p->n);
+    return fbc_cluster_eval_batch(p->G, (int32_t)p->coff.size() - 1, p->coff.data(), p->cverts.data(),
+                                  p->boff.empty() ? nullptr : p->boff.data(),
+                                  p->borders.empty() ? nullptr : p->borders.data(), p->prec,
+                                  FBC_SCHED_BATCHED, p->h_bc, p->h_bdist, p->h_bsig, st);
+}
+
+int fbc_plan_results(fbc_plan p, const double** intra_bc, const double** border_dist,
+                     const uint64_t** border_sigma, int64_t* entries, int32_t* captured) {
+    if (!p) return fail(FBC_ERR_INVALID_ARG, "null plan");
+    if (intra_bc) *intra_bc = p->h_bc;
+    if (border_dist) *border_dist = p->h_bdist;
+    if (border_sigma) *border_sigma = p->h_bsig;
+    if (entries) *entries = p->ent;
+    if (captured) *captured = p->captured ? 1 : 0;
+    return FBC_OK;
+}
+
+int fbc_plan_free(fbc_plan p) {
+    std::lock_guard<std::recursive_mutex> lk(g_mu);
+    if (!p) return FBC_OK;
+    if (g.init) cudaStreamSynchronize(g.st);
+    if (p->exec) cudaGraphExecDestroy(p->exec);
+    if (p->graph) cudaGraphDestroy(p->graph);
+    for (DBuf* b : {&p->crp, &p->cadj, &p->cgid, &p->cbord, &p->segs, &p->units, &p->chunks, &p->bc,
+                    &p->bdist, &p->bsig, &p->ctr, &p->retry})
+        b->release();
+    if (p->h_bc) cudaFreeHost(p->h_bc);
+    if (p->h_bdist) cudaFreeHost(p->h_bdist);
+    if (p->h_bsig) cudaFreeHost(p->h_bsig);
+    if (p->h_ctl) cudaFreeHost(p->h_ctl);
+    delete p;
     return FBC_OK;
 }
 

@@ -85,6 +85,10 @@ def _load():
                                     P(Stats)], C.c_int),
         "fbc_multi_exact_bc": ([i32, vp, C.c_int, C.c_int, vp, P(Stats)], C.c_int),
         "fbc_sssp_debug": ([vp, i32, vp, vp, vp, vp], C.c_int),
+        "fbc_cluster_plan_create": ([vp, i32, vp, vp, vp, vp, C.c_int, P(vp)], C.c_int),
+        "fbc_plan_run": ([vp, P(Stats)], C.c_int),
+        "fbc_plan_results": ([vp, P(vp), P(vp), P(vp), P(i64), P(i32)], C.c_int),
+        "fbc_plan_free": ([vp], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)
@@ -296,6 +300,55 @@ def cluster_eval_batch(g: Graph, cs: ClusterSet, precision: int = FP64, sched: i
                                    precision, sched, _ptr(intra_bc), _ptr(bd), _ptr(bs),
                                    _stats(stats)))
     return ClusterEval(intra_bc[: g.n], bd[:ent], bs[:ent], cs, entry_off)
+
+
+class ClusterPlan:
+    """A prepared cluster sweep (fbc_cluster_plan_create): the cluster subgraphs are uploaded
+    once and each run() replays a captured CUDA graph of the shared-memory kernel."""
+
+    def __init__(self, g: Graph, cs: ClusterSet, precision: int = FP64):
+        self.g = g
+        self.cs = cs.with_borders(g)
+        nb = np.diff(self.cs.boff)
+        self.entry_off = np.zeros(self.cs.count + 1, np.int64)
+        self.entry_off[1:] = np.cumsum(nb * np.diff(self.cs.off))
+        h = C.c_void_p()
+        bl = self.cs.borders if self.cs.borders.size else np.zeros(1, np.int32)
+        _ck(lib.fbc_cluster_plan_create(g._h, self.cs.count, _ptr(self.cs.off), _ptr(self.cs.vertices),
+                                        _ptr(self.cs.boff), _ptr(bl), precision, C.byref(h)))
+        self._h = h
+
+    @property
+    def captured(self) -> bool:
+        cap = C.c_int32()
+        _ck(lib.fbc_plan_results(self._h, None, None, None, None, C.byref(cap)))
+        return bool(cap.value)
+
+    def run(self, stats: Stats | None = None, copy: bool = True) -> ClusterEval:
+        """Replay the sweep.  With copy=False the returned arrays are views of the plan's pinned
+        buffers, overwritten by the next run."""
+        _ck(lib.fbc_plan_run(self._h, _stats(stats)))
+        bcp, bdp, bsp = C.c_void_p(), C.c_void_p(), C.c_void_p()
+        ent = C.c_int64()
+        _ck(lib.fbc_plan_results(self._h, C.byref(bcp), C.byref(bdp), C.byref(bsp), C.byref(ent), None))
+        n, e = self.g.n, int(ent.value)
+        bc = np.ctypeslib.as_array(C.cast(bcp, C.POINTER(C.c_double)), (max(n, 1),))[:n]
+        bd = np.ctypeslib.as_array(C.cast(bdp, C.POINTER(C.c_double)), (max(e, 1),))[:e]
+        bs = np.ctypeslib.as_array(C.cast(bsp, C.POINTER(C.c_uint64)), (max(e, 1),))[:e]
+        if copy:
+            bc, bd, bs = bc.copy(), bd.copy(), bs.copy()
+        return ClusterEval(bc, bd, bs, self.cs, self.entry_off)
+
+    def free(self) -> None:
+        if getattr(self, "_h", None):
+            lib.fbc_plan_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
 
 
 def multi_exact_bc(graphs: list[Graph], precision: int = FP64, sched: int = BATCHED,

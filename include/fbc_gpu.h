@@ -136,6 +136,23 @@ int fbc_cluster_eval_batch(fbc_graph g, int32_t nclusters, const int64_t* cluste
                            double* out_intra_bc, double* out_border_dist,
                            uint64_t* out_border_sigma, fbc_stats* st);
 
+/* Prepared cluster sweep for repeated evaluation of the same clusters (the Louvain-cluster
+ * sweep of the clustered mode): the cluster subgraphs, units and work items are uploaded once
+ * and the sweep (counter resets, the shared-memory kernel, downloads into pinned host buffers)
+ * is captured into a CUDA graph; fbc_plan_run replays it.  Clusters that do not fit the
+ * shared-memory kernel, or a run whose path counts need a wider representation, are evaluated
+ * with fbc_cluster_eval_batch instead (same results).  fbc_plan_results gives host views of the
+ * last run's intra-cluster BC (n entries, overwritten each run) and border vectors (layout of
+ * fbc_cluster_eval_batch), valid until the next run or fbc_plan_free. */
+typedef struct fbc_plan_s* fbc_plan;
+int fbc_cluster_plan_create(fbc_graph g, int32_t nclusters, const int64_t* cluster_off,
+                            const int32_t* cluster_vertices, const int64_t* border_off,
+                            const int32_t* borders, int precision, fbc_plan* out);
+int fbc_plan_run(fbc_plan p, fbc_stats* st);
+int fbc_plan_results(fbc_plan p, const double** intra_bc, const double** border_dist,
+                     const uint64_t** border_sigma, int64_t* entries, int32_t* captured);
+int fbc_plan_free(fbc_plan p);
+
 /* Exact BC of several independent graphs in one persistent launch.  out_bc[g] has
  * n_g entries. */
 int fbc_multi_exact_bc(int32_t ngraphs, const fbc_graph* graphs, int precision, int sched,

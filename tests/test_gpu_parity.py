@@ -255,6 +255,39 @@ def test_grid256_cluster_border_vectors(fg):
             assert np.array_equal(L, bd[i]) and np.array_equal(Cn.astype(np.float64), bs[i])
 
 
+@pytest.mark.parametrize("prec", [0, 1])
+def test_cluster_plan_replays(fg, prec):
+    """A prepared sweep (captured CUDA graph) gives the reference's intra BC and bit-exact border
+    vectors on every replay; with the shared-memory kernel ruled out it takes the general path
+    and gives the same results."""
+    z, keep, cs, piv, crd = _clustered_inputs(fg)
+    g = fg.Graph.from_edgelist(graphs.WORKLOADS["grid256"]())
+    tol = TOL_FP64 if prec == 0 else TOL_FP32C
+    base = fg.cluster_eval_batch(g, cs, prec, fg.PLAIN)
+    plan = fg.ClusterPlan(g, cs, prec)
+    assert plan.captured
+    for _ in range(3):
+        st = fg.Stats()
+        ev = plan.run(st)
+        assert st.launches == 1 and st.units == cs.vertices.size
+        assert rel_err(ev.intra_bc, z["intra_bc"]) <= tol
+        assert np.array_equal(ev.border_dist, base.border_dist)
+        assert np.array_equal(ev.border_sigma, base.border_sigma)
+    plan.free()
+    old = fg.get_option("warp_max_n")
+    fg.set_option("warp_max_n", 64)
+    try:
+        plan = fg.ClusterPlan(g, cs, prec)
+        assert not plan.captured
+        ev = plan.run()
+        assert rel_err(ev.intra_bc, z["intra_bc"]) <= tol
+        assert np.array_equal(ev.border_dist, base.border_dist)
+        assert np.array_equal(ev.border_sigma, base.border_sigma)
+        plan.free()
+    finally:
+        fg.set_option("warp_max_n", old)
+
+
 @pytest.mark.parametrize("sched", [0, 1])
 def test_grid256_sources_bit_exact_both_schedules(fg, sched):
     """Distances, path counts and predecessor counts from the plain block kernel and from the
