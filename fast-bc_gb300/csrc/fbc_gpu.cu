@@ -84,6 +84,7 @@ struct Options {
     int64_t warp_max_n = 4096;  // batched: segments up to this size run one source per warp
     int64_t iter_mult = 16;
     int64_t ws_budget_mb = 0;   // 0 = 60% of the free device memory
+    int64_t group = 0;          // frontier kernel sources per block (1, 2, 4); 0 = automatic
     int64_t warp_smem = 1;      // batched: warp state in shared memory when it fits
     int64_t debug_sched = FBC_SCHED_PLAIN;  // schedule used by fbc_sssp_debug
 };
@@ -106,7 +107,7 @@ struct Ctx {
     cudaStream_t st = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, evm = nullptr;
     Options opt;
-    DBuf retry, segs, units_b, units_w, chunks, crp, cadj, cgid, cbord, bc, bdist, bsig, ctr, dbg;
+    DBuf retry, segs, units_b, units_w, chunks, crp, cadj, cgid, cbord, bc, bdist, bsig, ctr, dbg, adjx;
     Workspace wsb, wsw;
 };
 Ctx g;
@@ -297,50 +298,118 @@ int64_t ws_budget() {
     return b + (int64_t)g.wsb.buf.cap + (int64_t)g.wsw.buf.cap;
 }
 
-// Block-per-source launch with global-memory slots.  Plain schedule: brandes_block_kernel;
-// batched schedule: frontier_kernel.
+using KernFn = void (*)(fbc::KParams);
+
 template <class Prec>
-int launch_block(const Plan& P, const std::vector<Unit>& units, int ws_n, fbc_stats* st,
+KernFn frontier_variant(bool wide, int K) {
+    if (wide) {
+        if (K == 4) return fbc::frontier_kernel<Prec, true, 4>;
+        if (K == 2) return fbc::frontier_kernel<Prec, true, 2>;
+        return fbc::frontier_kernel<Prec, true, 1>;
+    }
+    if (K == 4) return fbc::frontier_kernel<Prec, false, 4>;
+    if (K == 2) return fbc::frontier_kernel<Prec, false, 2>;
+    return fbc::frontier_kernel<Prec, false, 1>;
+}
+
+// Units of each segment in groups of K (a segment's last group padded with src = -1).
+std::vector<Unit> group_units(const std::vector<Unit>& units, int K) {
+    std::vector<Unit> out;
+    out.reserve(units.size() + (size_t)K * 8);
+    for (size_t i = 0; i < units.size();) {
+        size_t j = i;
+        while (j < units.size() && units[j].seg == units[i].seg) out.push_back(units[j++]);
+        while (out.size() % (size_t)K) out.push_back(Unit{units[i].seg, -1, 0.0, -1});
+        i = j;
+    }
+    return out;
+}
+
+// Block-per-source launch with global-memory slots.  Plain schedule: brandes_block_kernel;
+// batched schedule: frontier_kernel, K sources of one segment per block.
+template <class Prec>
+int launch_block(const Plan& P, const std::vector<Unit>& units_in, int ws_n, fbc_stats* st,
                  int& launches, bool force_plain = false, bool sig_f64 = false) {
-    if (units.empty()) return FBC_OK;
+    if (units_in.empty()) return FBC_OK;
     const bool fr = P.sched == FBC_SCHED_BATCHED && !force_plain && !sig_f64;
     // wide blocks for segments of millions of vertices (their frontiers are hundreds wide)
     const bool wide = fr && (g.opt.frontier_threads > 128 || (int64_t)ws_n >= g.opt.wide_n);
-    const int64_t sb = fr ? fbc::fstate_bytes<Prec>(ws_n) : fbc::state_bytes<Prec>(ws_n);
-    const int64_t stride = 256 + ((sb + 255) & ~int64_t(255));
     int threads = (int)std::min<int64_t>(std::max<int64_t>(fr ? g.opt.frontier_threads : g.opt.block_threads, 32),
                                          fr ? 128 : 1024);
     if (wide) threads = 512;
     threads = (threads / 32) * 32;
-    int bps = 0;
-    if (wide) FBC_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, fbc::frontier_kernel<Prec, true>, threads, 0));
-    else if (fr) FBC_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, fbc::frontier_kernel<Prec, false>, threads, 0));
-    else if (sig_f64) FBC_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, fbc::brandes_block_kernel<Prec, true>, threads, 0));
-    else FBC_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, fbc::brandes_block_kernel<Prec>, threads, 0));
-    bps = std::max(bps, 1);
-    int64_t slots = std::min<int64_t>((int64_t)g.nsm * bps, (int64_t)units.size());
-    slots = std::max<int64_t>(1, std::min<int64_t>(slots, ws_budget() / stride));
+    // units sorted so that each segment's units are adjacent (the caller sorts by size)
+    std::vector<Unit> sorted(units_in);
+    std::stable_sort(sorted.begin(), sorted.end(), [&](const Unit& a, const Unit& b) {
+        const int na = P.segs[a.seg].n, nb = P.segs[b.seg].n;
+        return na != nb ? na > nb : a.seg < b.seg;
+    });
+    KernFn kern = nullptr;
+    int Kg = 1, bps = 1;
+    int64_t stride = 0, slots = 0;
+    std::vector<Unit> units;
+    const int64_t budget = ws_budget();
+    if (fr) {
+        // sources per block: one unless option "group" asks for 2 or 4 (sharing rounds and
+        // levels pays only where a source's frontier is much narrower than the block; on
+        // road-like graphs one source per block measured faster at every size tried)
+        const int forced = (int)g.opt.group;
+        const int cand[3] = {4, 2, 1};
+        for (int K : cand) {
+            if (K != (forced > 0 ? forced : 1)) continue;
+            if ((int64_t)ws_n * K >= ((int64_t)1 << 31) - 1) continue;
+            KernFn f = frontier_variant<Prec>(wide, K);
+            int b = 0;
+            FBC_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, f, threads, 0));
+            b = std::max(b, 1);
+            const int64_t sb = fbc::fstate_bytes<Prec>((int64_t)ws_n * K);
+            const int64_t strd = 256 + ((sb + 255) & ~int64_t(255));
+            std::vector<Unit> gu = K > 1 ? group_units(sorted, K) : sorted;
+            const int64_t groups = (int64_t)gu.size() / K;
+            const int64_t full = (int64_t)g.nsm * b;
+            const int64_t sl = std::max<int64_t>(1, std::min<int64_t>(std::min(full, groups), budget / strd));
+            const bool ok = K == 1 || forced > 0 || (groups >= full && sl >= full);
+            if (!ok) continue;
+            kern = f;
+            Kg = K;
+            bps = b;
+            stride = strd;
+            slots = sl;
+            units.swap(gu);
+            break;
+        }
+    } else {
+        const int64_t sb = fbc::state_bytes<Prec>(ws_n);
+        stride = 256 + ((sb + 255) & ~int64_t(255));
+        kern = sig_f64 ? fbc::brandes_block_kernel<Prec, true> : fbc::brandes_block_kernel<Prec>;
+        FBC_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kern, threads, 0));
+        bps = std::max(bps, 1);
+        slots = std::min<int64_t>((int64_t)g.nsm * bps, (int64_t)sorted.size());
+        slots = std::max<int64_t>(1, std::min<int64_t>(slots, budget / stride));
+        units.swap(sorted);
+    }
+    if (!kern) return fail(FBC_ERR_INVALID_ARG, "no frontier kernel variant fits this segment");
     // the two kernels keep different between-unit invariants: never share a workspace
     Workspace& W = fr ? g.wsw : g.wsb;
-    FBC_TRY(ensure_ws(W, slots, stride, ws_n, (int)sizeof(typename Prec::D)));
+    FBC_TRY(ensure_ws(W, slots, stride, ws_n * Kg, (int)sizeof(typename Prec::D)));
     FBC_CK(g.units_b.ensure(sizeof(Unit) * units.size()));
     FBC_CK(cudaMemcpyAsync(g.units_b.p, units.data(), sizeof(Unit) * units.size(),
                            cudaMemcpyHostToDevice, g.st));
     if (st) st->h2d_bytes += (int64_t)(sizeof(Unit) * units.size());
     KParams K = base_params(P);
     K.units = g.units_b.as<Unit>();
-    K.nunits = (int64_t)units.size();
+    K.nunits = (int64_t)units.size() / Kg;
     K.next_unit = g.ctr.as<unsigned long long>() + 0;
     K.ws = W.buf.as<char>();
     K.ws_stride = W.stride;
-    K.ws_n = W.ws_n;
-    if (wide) fbc::frontier_kernel<Prec, true><<<(unsigned)slots, threads, 0, g.st>>>(K);
-    else if (fr) fbc::frontier_kernel<Prec, false><<<(unsigned)slots, threads, 0, g.st>>>(K);
-    else if (sig_f64) fbc::brandes_block_kernel<Prec, true><<<(unsigned)slots, threads, 0, g.st>>>(K);
-    else fbc::brandes_block_kernel<Prec><<<(unsigned)slots, threads, 0, g.st>>>(K);
+    K.ws_n = (int32_t)W.ws_n;  // block kernel: vertices; frontier kernel: entries (v*K + k)
+    kern<<<(unsigned)slots, threads, 0, g.st>>>(K);
     FBC_CK(cudaGetLastError());
     ++launches;
-    if (st) st->slots = (int32_t)slots;
+    if (st) {
+        st->slots = (int32_t)slots;
+        st->group = Kg;
+    }
     return FBC_OK;
 }
 
@@ -434,9 +503,6 @@ int map_err(int e) {
 // (g.bc, g.bdist, g.bsig) for the caller to download.
 template <class Prec>
 int run_plan_t(Plan& P, fbc_stats* st) {
-    FBC_CK(g.segs.ensure(sizeof(Seg) * std::max<size_t>(P.segs.size(), 1)));
-    FBC_CK(cudaMemcpyAsync(g.segs.p, P.segs.data(), sizeof(Seg) * P.segs.size(),
-                           cudaMemcpyHostToDevice, g.st));
     FBC_CK(g.bc.ensure(sizeof(double) * std::max<int64_t>(P.bc_len, 1)));
     FBC_CK(cudaMemsetAsync(g.bc.p, 0, sizeof(double) * std::max<int64_t>(P.bc_len, 1), g.st));
     FBC_CK(g.bdist.ensure(sizeof(double) * std::max<int64_t>(P.border_entries, 1)));
@@ -493,6 +559,31 @@ int run_plan_t(Plan& P, fbc_stats* st) {
                 P.sched = FBC_SCHED_PLAIN;
                 break;
             }
+    // the frontier kernel reads each segment's annotated adjacency
+    if (P.sched == FBC_SCHED_BATCHED && !ub.empty()) {
+        std::vector<int64_t> xoff(P.segs.size(), -1);
+        int64_t tot = 0;
+        for (const Unit& u : ub)
+            if (xoff[u.seg] < 0) {
+                xoff[u.seg] = tot;
+                tot += P.seg_m[u.seg];
+            }
+        FBC_CK(g.adjx.ensure(sizeof(int4) * (size_t)std::max<int64_t>(tot, 1)));
+        for (size_t s = 0; s < P.segs.size(); ++s)
+            if (xoff[s] >= 0) {
+                int4* dst = g.adjx.as<int4>() + xoff[s];
+                if (P.seg_m[s] > 0) {
+                    const int64_t blocks = std::min<int64_t>((P.seg_m[s] + 255) / 256, (int64_t)g.nsm * 8);
+                    fbc::build_adjx_kernel<<<(unsigned)blocks, 256, 0, g.st>>>(P.segs[s].rp, P.segs[s].adj,
+                                                                             P.seg_m[s], dst);
+                    FBC_CK(cudaGetLastError());
+                }
+                P.segs[s].adjx = dst;
+            }
+    }
+    FBC_CK(g.segs.ensure(sizeof(Seg) * std::max<size_t>(P.segs.size(), 1)));
+    FBC_CK(cudaMemcpyAsync(g.segs.p, P.segs.data(), sizeof(Seg) * P.segs.size(),
+                           cudaMemcpyHostToDevice, g.st));
     int launches = 0;
     FBC_CK(cudaEventRecord(g.ev0, g.st));
     FBC_CK(g.retry.ensure(sizeof(fbc::RetryRec) * std::max<size_t>(P.units.size(), 1)));
@@ -749,7 +840,7 @@ int fbc_gpu_shutdown(void) {
     std::lock_guard<std::recursive_mutex> lk(g_mu);
     if (!g.init) return FBC_OK;
     cudaStreamSynchronize(g.st);
-    for (DBuf* b : {&g.retry, &g.segs, &g.units_b, &g.units_w, &g.chunks, &g.crp, &g.cadj, &g.cgid, &g.cbord, &g.bc,
+    for (DBuf* b : {&g.adjx, &g.retry, &g.segs, &g.units_b, &g.units_w, &g.chunks, &g.crp, &g.cadj, &g.cgid, &g.cbord, &g.bc,
                     &g.bdist, &g.bsig, &g.ctr, &g.dbg})
         b->release();
     g.wsb.buf.release();
@@ -776,6 +867,10 @@ int fbc_set_option(const char* key, int64_t value) {
     else if (k == "warp_max_n") g.opt.warp_max_n = std::max<int64_t>(0, value);
     else if (k == "iter_mult") g.opt.iter_mult = std::max<int64_t>(1, std::min<int64_t>(1 << 20, value));
     else if (k == "ws_budget_mb") g.opt.ws_budget_mb = std::max<int64_t>(0, value);
+    else if (k == "group") {
+        if (value != 0 && value != 1 && value != 2 && value != 4) return fail(FBC_ERR_INVALID_ARG, "group must be 0, 1, 2 or 4");
+        g.opt.group = value;
+    }
     else if (k == "warp_smem") g.opt.warp_smem = value ? 1 : 0;
     else if (k == "debug_sched") g.opt.debug_sched = value ? FBC_SCHED_BATCHED : FBC_SCHED_PLAIN;
     else return fail(FBC_ERR_INVALID_ARG, "unknown option " + k);
@@ -794,6 +889,7 @@ int fbc_get_option(const char* key, int64_t* value) {
     else if (k == "warp_max_n") *value = g.opt.warp_max_n;
     else if (k == "iter_mult") *value = g.opt.iter_mult;
     else if (k == "ws_budget_mb") *value = g.opt.ws_budget_mb;
+    else if (k == "group") *value = g.opt.group;
     else if (k == "warp_smem") *value = g.opt.warp_smem;
     else if (k == "debug_sched") *value = g.opt.debug_sched;
     else return fail(FBC_ERR_INVALID_ARG, "unknown option " + k);

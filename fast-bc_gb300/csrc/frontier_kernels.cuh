@@ -37,15 +37,22 @@ struct LEnt {
 // graphs are far smaller than n: they get qcap entries, and a unit that would overflow them is
 // handed to the plain kernel (whose queues hold n).
 __host__ __device__ inline int64_t fqcap(int64_t cap) {
-    const int64_t q = cap / 4 + 1 > 65536 ? cap / 4 + 1 : 65536;
+    const int64_t q = cap / 8 + 1 > 65536 ? cap / 8 + 1 : 65536;
     return q < cap + 1 ? q : cap + 1;
 }
+
+// Path count and dependency of a vertex side by side, so the dependency pass reads both with
+// one 16-byte load.
+template <class Prec>
+struct __align__(16) FRec {
+    unsigned long long sc;        // (sigma << 16 | tight in-edges still unprocessed)
+    typename Prec::D dlt;
+};
 
 template <class Prec>
 struct FState {
     unsigned long long* word;     // (dist << 32 | queue stamp)
-    unsigned long long* sc;       // (sigma << 16 | tight in-edges still unprocessed)
-    typename Prec::D* dlt;
+    FRec<Prec>* rec;
     QEnt* q[4];                   // near0, near1, far0, far1 (fqcap(cap) entries)
     LEnt* order;                  // cap + 1 entries
     int* lvl;                     // cap + 1 entries
@@ -55,8 +62,7 @@ struct FState {
 template <class Prec>
 __host__ __device__ inline int64_t fstate_bytes(int64_t cap) {
     auto al = [](int64_t x) { return (x + 255) & ~int64_t(255); };
-    return al(cap * 8) + al(cap * 8) + al(cap * (int64_t)sizeof(typename Prec::D)) +
-           4 * al(fqcap(cap) * (int64_t)sizeof(QEnt)) + al((cap + 1) * (int64_t)sizeof(LEnt)) +
+    return al(cap * 8) + al(cap * (int64_t)sizeof(FRec<Prec>)) + 4 * al(fqcap(cap) * (int64_t)sizeof(QEnt)) + al((cap + 1) * (int64_t)sizeof(LEnt)) +
            al((cap + 1) * 4) + al(cap * 4);
 }
 
@@ -65,8 +71,7 @@ __device__ inline FState<Prec> fstate_carve(char* p, int64_t cap) {
     auto al = [](int64_t x) { return (x + 255) & ~int64_t(255); };
     FState<Prec> s;
     s.word = (unsigned long long*)p; p += al(cap * 8);
-    s.sc = (unsigned long long*)p; p += al(cap * 8);
-    s.dlt = (typename Prec::D*)p; p += al(cap * (int64_t)sizeof(typename Prec::D));
+    s.rec = (FRec<Prec>*)p; p += al(cap * (int64_t)sizeof(FRec<Prec>));
     for (int i = 0; i < 4; ++i) { s.q[i] = (QEnt*)p; p += al(fqcap(cap) * (int64_t)sizeof(QEnt)); }
     s.order = (LEnt*)p; p += al((cap + 1) * (int64_t)sizeof(LEnt));
     s.lvl = (int*)p; p += al((cap + 1) * 4);
@@ -89,6 +94,29 @@ struct FCtl {
 constexpr unsigned long long kSigMax = (1ull << 48) - 1ull;
 
 __device__ __forceinline__ unsigned long long ldcg64(const unsigned long long* p) { return __ldcg(p); }
+
+// The 8 bytes of a dependency value read as part of a 16-byte record load.
+template <class D>
+__device__ __forceinline__ D bits_to(unsigned long long b);
+template <>
+__device__ __forceinline__ double bits_to<double>(unsigned long long b) {
+    return __longlong_as_double((long long)b);
+}
+template <>
+__device__ __forceinline__ float2 bits_to<float2>(unsigned long long b) {
+    return make_float2(__int_as_float((int)(unsigned)b), __int_as_float((int)(unsigned)(b >> 32)));
+}
+
+// Annotated adjacency of one segment: (x, w, rp[x], rp[x+1] - rp[x]) for every edge, so that a
+// relaxation that pushes x already holds x's row.
+__global__ void build_adjx_kernel(const int* __restrict__ rp, const int2* __restrict__ adj, int64_t m,
+                                  int4* __restrict__ out) {
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < m; e += (int64_t)gridDim.x * blockDim.x) {
+        const int2 a = adj[e];
+        const int r0 = __ldg(rp + a.x), r1 = __ldg(rp + a.x + 1);
+        out[e] = make_int4(a.x, a.y, r0, r1 - r0);
+    }
+}
 __device__ __forceinline__ int dist_of(unsigned long long w) { return (int)(w >> 32); }
 
 // Block-wide push (warp-aggregated slot reservation on a shared-memory counter); a push past
@@ -109,14 +137,24 @@ __device__ __forceinline__ void bpush(bool want, const E& x, E* q, int* c, int c
     }
 }
 
-template <class Prec>
-__device__ void frontier_unit(const KParams& P, int64_t ui, const Unit& u, const FState<Prec>& S,
-                              FCtl& C, int cap) {
-    const Seg sg = P.segs[u.seg];
+// One group of K sources of the same segment per block: the sources share the distance
+// rounds, the Kahn levels and the dependency levels (one barrier per round or level for all
+// of them), and their per-vertex state is interleaved, entry v*K + k for source k, so the
+// words of nearby sources' wavefronts share sectors and the adjacency rows they read are the
+// same.  Queue and level entries name an entry vk = v*K + k.  K = 1 is one source per block.
+// kV: vertices per lane in the Kahn and dependency passes (4 for the wide blocks of
+// million-vertex graphs, whose levels are thousands wide; 1 for the narrow blocks).
+template <class Prec, int kV, int K>
+__device__ void frontier_group(const KParams& P, const Unit* us, const FState<Prec>& S, FCtl& C,
+                               int64_t cap) {
+    static_assert(K == 1 || K == 2 || K == 4 || K == 8, "K is a power of two up to 8");
+    constexpr int kSh = K == 1 ? 0 : K == 2 ? 1 : K == 4 ? 2 : 3;
+    const Seg sg = P.segs[us[0].seg];
     const int n = sg.n;
+    const int nK = n * K;
     const int* __restrict__ rp = sg.rp;
     const int2* __restrict__ adj = sg.adj;
-    const int src = u.src;
+    const int4* __restrict__ adjx = sg.adjx;
     const int delta = sg.delta > 0 ? sg.delta : 1;
     const int tid = threadIdx.x, nth = blockDim.x;
     const int qc_cap = (int)fqcap(cap);
@@ -127,10 +165,15 @@ __device__ void frontier_unit(const KParams& P, int64_t ui, const Unit& u, const
     int qs = 0, fs = 0;
     unsigned stamp = 1u, fst = 1u;
     if (tid == 0) {
-        S.word[src] = 0ull;  // dist 0, stamp 0
-        const int e0 = __ldg(rp + src);
-        S.q[0][0] = QEnt{src, e0, __ldg(rp + src + 1) - e0, 0};
-        C.ncnt[0] = 1;
+        int c = 0;
+        for (int k = 0; k < K; ++k) {
+            const int src = us[k].src;
+            if (src < 0) continue;
+            S.word[src * K + k] = 0ull;  // dist 0, stamp 0
+            const int e0 = __ldg(rp + src);
+            S.q[0][c++] = QEnt{src * K + k, e0, __ldg(rp + src + 1) - e0, 0};
+        }
+        C.ncnt[0] = c;
         C.ncnt[1] = 0;
         C.fcnt[0] = 0;
         C.fcnt[1] = 0;
@@ -150,44 +193,44 @@ __device__ void frontier_unit(const KParams& P, int64_t ui, const Unit& u, const
             // warp-uniform trip count so that every lane reaches the ballots
             for (int base = tid & ~31; base < ncur; base += nth) {
                 const int i = base + (tid & 31);
-                int e = 0, e1 = 0, dv = 0;
+                int e = 0, e1 = 0, dv = 0, k = 0;
                 if (i < ncur) {
                     const QEnt q = qc[i];
                     e = q.e0;
                     e1 = q.e0 + q.deg;
+                    k = q.v & (K - 1);
                     dv = dist_of(ldcg64(S.word + q.v));  // may have dropped since the push
                 }
                 while (__any_sync(kFull, e < e1)) {
                     int x[4], nd[4], r0[4], r1[4];
                     unsigned long long old[4];
 #pragma unroll
-                    for (int k = 0; k < 4; ++k) {
-                        x[k] = -1;
-                        if (e + k < e1) {
-                            const int2 a = __ldg(adj + e + k);
-                            x[k] = a.x;
-                            nd[k] = dv + a.y;
+                    for (int j = 0; j < 4; ++j) {
+                        x[j] = -1;
+                        if (e + j < e1) {
+                            const int4 a = __ldg(adjx + e + j);  // (x, w, x's row start, x's degree)
+                            x[j] = (a.x << kSh) + k;
+                            nd[j] = dv + a.y;
+                            r0[j] = a.z;
+                            r1[j] = a.z + a.w;
                         }
                     }
 #pragma unroll
-                    for (int k = 0; k < 4; ++k)
-                        if (x[k] >= 0) {
-                            old[k] = atomicMin(S.word + x[k],
-                                               ((unsigned long long)(unsigned)nd[k] << 32) | (nd[k] < T ? nst : fst));
-                            r0[k] = __ldg(rp + x[k]);      // in flight with the atomic
-                            r1[k] = __ldg(rp + x[k] + 1);
-                        }
+                    for (int j = 0; j < 4; ++j)
+                        if (x[j] >= 0)
+                            old[j] = atomicMin(S.word + x[j],
+                                               ((unsigned long long)(unsigned)nd[j] << 32) | (nd[j] < T ? nst : fst));
 #pragma unroll
-                    for (int k = 0; k < 4; ++k) {
+                    for (int j = 0; j < 4; ++j) {
                         bool pn = false, pf = false;
-                        if (x[k] >= 0) {
-                            const bool near = nd[k] < T;
-                            if (nd[k] < dist_of(old[k]) && (unsigned)old[k] != (near ? nst : fst)) {
+                        if (x[j] >= 0) {
+                            const bool near = nd[j] < T;
+                            if (nd[j] < dist_of(old[j]) && (unsigned)old[j] != (near ? nst : fst)) {
                                 pn = near;
                                 pf = !near;
                             }
                         }
-                        const QEnt qe{x[k], r0[k], r1[k] - r0[k], 0};
+                        const QEnt qe{x[j], r0[j], r1[j] - r0[j], 0};
                         bpush(pn, qe, qnx, &C.ncnt[qs ^ 1], qc_cap, &C.ovf);
                         bpush(pf, qe, qfx, &C.fcnt[fs], qc_cap, &C.ovf);
                     }
@@ -228,7 +271,7 @@ __device__ void frontier_unit(const KParams& P, int64_t ui, const Unit& u, const
             if (i < nfar) {
                 qe = qfc[i];
                 const int d = dist_of(ldcg64(S.word + qe.v));
-                if (d >= Told) {  // the far pile holds a vertex once per generation
+                if (d >= Told) {  // the far pile holds an entry once per generation
                     pn = d < T;
                     pf = !pn;
                     S.word[qe.v] = ((unsigned long long)(unsigned)d << 32) | (pn ? nsplit : fst);
@@ -248,22 +291,23 @@ __device__ void frontier_unit(const KParams& P, int64_t ui, const Unit& u, const
     int nlev = 0;
     if (!bad) {
         // ------------------------------------------------------------- sigma (Kahn)
-        // tight in-edge counts and each vertex's tight out-edge mask: a sweep over all
-        // vertices, four per thread in flight
-        for (int v0 = tid; v0 < n; v0 += 4 * nth) {
+        // tight in-edge counts and each entry's tight out-edge mask: a sweep over all
+        // entries, four per thread in flight; the K entries of a vertex sit on adjacent lanes,
+        // so their row and neighbour-word loads coalesce
+        for (int v0 = tid; v0 < nK; v0 += 4 * nth) {
             int dv[4], e[4], e1[4], eb[4];
             unsigned mk[4];
 #pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                const int v = v0 + k * nth;
-                dv[k] = kInf;
-                e[k] = e1[k] = eb[k] = 0;
-                mk[k] = 0u;
-                if (v < n) {
-                    dv[k] = dist_of(ldcg64(S.word + v));
-                    if (dv[k] != kInf) {
-                        e[k] = eb[k] = __ldg(rp + v);
-                        e1[k] = __ldg(rp + v + 1);
+            for (int j = 0; j < 4; ++j) {
+                const int vk = v0 + j * nth;
+                dv[j] = kInf;
+                e[j] = e1[j] = eb[j] = 0;
+                mk[j] = 0u;
+                if (vk < nK) {
+                    dv[j] = dist_of(ldcg64(S.word + vk));
+                    if (dv[j] != kInf) {
+                        e[j] = eb[j] = __ldg(rp + (vk >> kSh));
+                        e1[j] = __ldg(rp + (vk >> kSh) + 1);
                     }
                 }
             }
@@ -271,101 +315,128 @@ __device__ void frontier_unit(const KParams& P, int64_t ui, const Unit& u, const
                 int x[4], nd[4];
                 bool any = false;
 #pragma unroll
-                for (int k = 0; k < 4; ++k) {
-                    x[k] = -1;
-                    if (e[k] < e1[k]) {
-                        const int2 a = __ldg(adj + e[k]++);
-                        x[k] = a.x;
-                        nd[k] = dv[k] + a.y;
+                for (int j = 0; j < 4; ++j) {
+                    x[j] = -1;
+                    if (e[j] < e1[j]) {
+                        const int2 a = __ldg(adj + e[j]++);
+                        x[j] = (a.x << kSh) + ((v0 + j * nth) & (K - 1));
+                        nd[j] = dv[j] + a.y;
                         any = true;
                     }
                 }
                 if (!any) break;
                 int dx[4];
 #pragma unroll
-                for (int k = 0; k < 4; ++k) dx[k] = x[k] >= 0 ? dist_of(ldcg64(S.word + x[k])) : -1;
+                for (int j = 0; j < 4; ++j) dx[j] = x[j] >= 0 ? dist_of(ldcg64(S.word + x[j])) : -1;
 #pragma unroll
-                for (int k = 0; k < 4; ++k)
-                    if (x[k] >= 0 && nd[k] == dx[k]) {
-                        atomicAdd(S.sc + x[k], 1ull);
-                        const int bit = e[k] - 1 - eb[k];
-                        if (bit < 32) mk[k] |= 1u << bit;
+                for (int j = 0; j < 4; ++j)
+                    if (x[j] >= 0 && nd[j] == dx[j]) {
+                        atomicAdd(&S.rec[x[j]].sc, 1ull);
+                        const int bit = e[j] - 1 - eb[j];
+                        if (bit < 32) mk[j] |= 1u << bit;
                     }
             }
 #pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                const int v = v0 + k * nth;
-                if (v < n && dv[k] != kInf) S.tmask[v] = e1[k] - eb[k] > 32 ? 0xffffffffu : mk[k];
+            for (int j = 0; j < 4; ++j) {
+                const int vk = v0 + j * nth;
+                if (vk < nK && dv[j] != kInf) S.tmask[vk] = e1[j] - eb[j] > 32 ? 0xffffffffu : mk[j];
             }
         }
         __syncthreads();
         if (tid == 0) {
-            const int e0 = __ldg(rp + src);
-            S.order[0] = LEnt{src, 0, e0, __ldcg(S.tmask + src), 1ull};
+            int c = 0;
+            for (int k = 0; k < K; ++k) {
+                const int src = us[k].src;
+                if (src < 0) continue;
+                S.order[c++] = LEnt{src * K + k, 0, __ldg(rp + src), __ldcg(S.tmask + src * K + k), 1ull};
+            }
             S.lvl[0] = 0;
-            C.ocnt = 1;
+            C.ocnt = c;
         }
         __syncthreads();
-        int lo = 0, hi = 1;
+        int lo = 0, hi = C.ocnt;
         while (lo < hi) {
             if (nlev >= n) { bad = kErrIter; break; }
-            for (int base = lo + (tid & ~31); base < hi; base += nth) {
-                const int i = base + (tid & 31);
-                int dv = 0, e0 = 0, e = 0, e1 = 0;
-                unsigned mk = 0u;
-                unsigned long long sv = 0;
-                if (i < hi) {
-                    const LEnt o = S.order[i];
-                    dv = o.d;
-                    sv = o.sig;
-                    e0 = o.e0;
-                    mk = o.dm;
-                    if (mk == 0xffffffffu) {  // long row: walk it and re-test every edge
-                        e = e0;
-                        e1 = __ldg(rp + o.v + 1);
-                        mk = 0u;
+            // each lane takes kV entries of the level (coalesced: entries j*32 + lane of the
+            // warp's span) and issues one tight edge of each per step, so kV atomics are in
+            // flight together (the DAG of a road-like graph has about one tight out-edge per
+            // vertex)
+            for (int base = lo + (tid & ~31) * kV; base < hi; base += nth * kV) {
+                int dv[kV], e0[kV], e[kV], e1[kV], kk[kV];
+                unsigned mk[kV];
+                unsigned long long sv[kV];
+#pragma unroll
+                for (int j = 0; j < kV; ++j) {
+                    const int i = base + j * 32 + (tid & 31);
+                    dv[j] = e0[j] = e[j] = e1[j] = kk[j] = 0;
+                    mk[j] = 0u;
+                    sv[j] = 0ull;
+                    if (i < hi) {
+                        const LEnt o = S.order[i];
+                        dv[j] = o.d;
+                        sv[j] = o.sig;
+                        e0[j] = o.e0;
+                        mk[j] = o.dm;
+                        kk[j] = o.v & (K - 1);
+                        if (mk[j] == 0xffffffffu) {  // long row: walk it and re-test every edge
+                            e[j] = o.e0;
+                            e1[j] = __ldg(rp + (o.v >> kSh) + 1);
+                            mk[j] = 0u;
+                        }
                     }
                 }
-                while (__any_sync(kFull, mk != 0u || e < e1)) {
-                    int x[4], nd[4];
-                    bool tight[4];
+                for (;;) {
+                    bool more = false;
 #pragma unroll
-                    for (int k = 0; k < 4; ++k) {
-                        x[k] = -1;
-                        tight[k] = false;
+                    for (int j = 0; j < kV; ++j) more |= mk[j] != 0u || e[j] < e1[j];
+                    if (!__any_sync(kFull, more)) break;
+                    int x[kV], nd[kV], r0[kV];
+                    bool tight[kV];
+#pragma unroll
+                    for (int j = 0; j < kV; ++j) {
+                        x[j] = -1;
+                        tight[j] = false;
                         int ei = -1;
-                        if (mk) {  // tight by the counting sweep
-                            ei = e0 + __ffs(mk) - 1;
-                            mk &= mk - 1u;
-                            tight[k] = true;
-                        } else if (e < e1) {
-                            ei = e++;
+                        if (mk[j]) {  // tight by the counting sweep
+                            ei = e0[j] + __ffs(mk[j]) - 1;
+                            mk[j] &= mk[j] - 1u;
+                            tight[j] = true;
+                        } else if (e[j] < e1[j]) {
+                            ei = e[j]++;
                         }
                         if (ei >= 0) {
-                            const int2 a = __ldg(adj + ei);
-                            x[k] = a.x;
-                            nd[k] = dv + a.y;
+                            const int4 a = __ldg(adjx + ei);  // x's row start comes along
+                            x[j] = (a.x << kSh) + kk[j];
+                            nd[j] = dv[j] + a.y;
+                            r0[j] = a.z;
                         }
                     }
 #pragma unroll
-                    for (int k = 0; k < 4; ++k)
-                        if (x[k] >= 0 && !tight[k]) tight[k] = nd[k] == dist_of(ldcg64(S.word + x[k]));
+                    for (int j = 0; j < kV; ++j)
+                        if (x[j] >= 0 && !tight[j]) tight[j] = nd[j] == dist_of(ldcg64(S.word + x[j]));
+                    unsigned long long old[kV];
+                    unsigned tm[kV];
 #pragma unroll
-                    for (int k = 0; k < 4; ++k) {
-                        bool push = false;
-                        LEnt le{x[k], nd[k], 0, 0u, 0ull};
-                        if (tight[k]) {
+                    for (int j = 0; j < kV; ++j)
+                        if (tight[j]) {
                             // one atomic adds sigma_v and retires the edge; the thread that
                             // retires the last tight in-edge knows x's final count
-                            const unsigned long long old = atomicAdd(S.sc + x[k], (sv << 16) - 1ull);
-                            const unsigned long long sx = (old >> 16) + sv;
-                            if (sx > kSigMax || sv > kSigMax) bad |= kErrRetry;
-                            push = (old & 0xffffull) == 1ull;
-                            le.sig = sx;
-                            le.e0 = __ldg(rp + x[k]);        // in flight with the atomic
-                            le.dm = __ldcg(S.tmask + x[k]);
+                            old[j] = atomicAdd(&S.rec[x[j]].sc, (sv[j] << 16) - 1ull);
+                            tm[j] = __ldcg(S.tmask + x[j]);  // in flight with the atomic
                         }
-                        bpush(push, le, S.order, &C.ocnt, cap + 1, &C.ovf);
+#pragma unroll
+                    for (int j = 0; j < kV; ++j) {
+                        bool push = false;
+                        LEnt le{x[j], nd[j], 0, 0u, 0ull};
+                        if (tight[j]) {
+                            const unsigned long long sx = (old[j] >> 16) + sv[j];
+                            if (sx > kSigMax || sv[j] > kSigMax) bad |= kErrRetry;
+                            push = (old[j] & 0xffffull) == 1ull;
+                            le.sig = sx;
+                            le.e0 = r0[j];
+                            le.dm = tm[j];
+                        }
+                        bpush(push, le, S.order, &C.ocnt, (int)cap + 1, &C.ovf);
                     }
                 }
             }
@@ -382,107 +453,139 @@ __device__ void frontier_unit(const KParams& P, int64_t ui, const Unit& u, const
         if (bad) atomicOr(&C.bad, bad);
         __syncthreads();
         bad = C.bad;
-        if (!bad && u.bout >= 0) {
-            for (int j = tid; j < sg.nb; j += nth) {
-                const int b = sg.border[j];
-                const int d = dist_of(ldcg64(S.word + b));
-                P.bdist[u.bout + j] = d != kInf ? (double)d : 0.0;
-                P.bsig[u.bout + j] = d != kInf ? (d == 0 ? 1ull : __ldcg(S.sc + b) >> 16) : 0ull;
+        if (!bad) {
+            for (int k = 0; k < K; ++k) {
+                const Unit& u = us[k];
+                if (u.src < 0 || u.bout < 0) continue;
+                for (int j = tid; j < sg.nb; j += nth) {
+                    const int b = sg.border[j] * K + k;
+                    const int d = dist_of(ldcg64(S.word + b));
+                    P.bdist[u.bout + j] = d != kInf ? (double)d : 0.0;
+                    P.bsig[u.bout + j] = d != kInf ? (d == 0 ? 1ull : __ldcg(&S.rec[b].sc) >> 16) : 0ull;
+                }
             }
         }
     }
     if (!bad) {
         // --------------------------------------------------------- dependency
-        const double card = u.card;
         for (int L = nlev - 1; L >= 0; --L) {
             const int a0 = __ldcg(S.lvl + L), a1 = __ldcg(S.lvl + L + 1);
-            for (int i = a0 + tid; i < a1; i += nth) {
-                const LEnt o = S.order[i];
-                const int v = o.v, dv = o.d;
-                const unsigned long long sv = o.sig;
-                typename Prec::Acc acc = Prec::zero();
-                if (o.dm != 0xffffffffu) {
-                    // tight out-edges only, four at a time (the mask was set by the Kahn pass)
-                    unsigned mk = o.dm;
-                    while (mk) {
-                        int x[4];
+            // kV entries per lane, one tight edge of each per step (as in the Kahn pass)
+            for (int base = a0 + (tid & ~31) * kV; base < a1; base += nth * kV) {
+                LEnt o[kV];
+                unsigned mk[kV];
+                typename Prec::Acc acc[kV];
 #pragma unroll
-                        for (int k = 0; k < 4; ++k) {
-                            x[k] = -1;
-                            if (mk) {
-                                const int b = __ffs(mk) - 1;
-                                mk &= mk - 1u;
-                                x[k] = __ldg(adj + o.e0 + b).x;
-                            }
-                        }
-                        unsigned long long sx[4];
-                        typename Prec::D dx[4];
-#pragma unroll
-                        for (int k = 0; k < 4; ++k)
-                            if (x[k] >= 0) {
-                                sx[k] = __ldcg(S.sc + x[k]) >> 16;
-                                dx[k] = S.dlt[x[k]];
-                            }
-#pragma unroll
-                        for (int k = 0; k < 4; ++k)
-                            if (x[k] >= 0) {
-                                if (sx[k] == sv) Prec::add_same(acc, dx[k]);
-                                else Prec::add(acc, sv, sx[k], dx[k]);
-                            }
-                    }
-                } else {
-                    const int e1 = __ldg(rp + v + 1);
-                    for (int e = o.e0; e < e1; ++e) {
-                        const int2 a = __ldg(adj + e);
-                        if (dv + a.y == dist_of(ldcg64(S.word + a.x))) {
-                            const unsigned long long sx = __ldcg(S.sc + a.x) >> 16;
-                            if (sx == sv) Prec::add_same(acc, S.dlt[a.x]);
-                            else Prec::add(acc, sv, sx, S.dlt[a.x]);
-                        }
+                for (int j = 0; j < kV; ++j) {
+                    const int i = base + j * 32 + (tid & 31);
+                    acc[j] = Prec::zero();
+                    o[j].v = -1;
+                    mk[j] = 0u;
+                    if (i < a1) {
+                        o[j] = S.order[i];
+                        mk[j] = o[j].dm == 0xffffffffu ? 0u : o[j].dm;
                     }
                 }
-                S.dlt[v] = Prec::store(acc);
-                if (v != src) {
-                    const int64_t ov = sg.gid ? (int64_t)sg.gid[v] : sg.out_base + v;
-                    atomicAdd(P.bc + ov, card == 1.0 ? Prec::value(acc) : card * Prec::value(acc));
+                for (;;) {
+                    bool more = false;
+#pragma unroll
+                    for (int j = 0; j < kV; ++j) more |= mk[j] != 0u;
+                    if (!more) break;
+                    int x[kV];
+#pragma unroll
+                    for (int j = 0; j < kV; ++j) {
+                        x[j] = -1;
+                        if (mk[j]) {
+                            const int b = __ffs(mk[j]) - 1;
+                            mk[j] &= mk[j] - 1u;
+                            x[j] = (__ldg(adj + o[j].e0 + b).x << kSh) + (o[j].v & (K - 1));
+                        }
+                    }
+                    unsigned long long sx[kV];
+                    typename Prec::D dx[kV];
+#pragma unroll
+                    for (int j = 0; j < kV; ++j)
+                        if (x[j] >= 0) {
+                            const ulonglong2 r = __ldcg(reinterpret_cast<const ulonglong2*>(S.rec + x[j]));
+                            sx[j] = r.x >> 16;
+                            dx[j] = bits_to<typename Prec::D>(r.y);
+                        }
+#pragma unroll
+                    for (int j = 0; j < kV; ++j)
+                        if (x[j] >= 0) {
+                            if (sx[j] == o[j].sig) Prec::add_same(acc[j], dx[j]);
+                            else Prec::add(acc[j], o[j].sig, sx[j], dx[j]);
+                        }
+                }
+#pragma unroll
+                for (int j = 0; j < kV; ++j) {
+                    if (o[j].v < 0) continue;
+                    const int v = o[j].v >> kSh, k = o[j].v & (K - 1);
+                    if (o[j].dm == 0xffffffffu) {  // long row: re-test every edge
+                        const int e1 = __ldg(rp + v + 1);
+                        for (int e = o[j].e0; e < e1; ++e) {
+                            const int2 a = __ldg(adj + e);
+                            const int xk = (a.x << kSh) + k;
+                            if (o[j].d + a.y == dist_of(ldcg64(S.word + xk))) {
+                                const ulonglong2 r = __ldcg(reinterpret_cast<const ulonglong2*>(S.rec + xk));
+                                const unsigned long long s2 = r.x >> 16;
+                                const typename Prec::D d2 = bits_to<typename Prec::D>(r.y);
+                                if (s2 == o[j].sig) Prec::add_same(acc[j], d2);
+                                else Prec::add(acc[j], o[j].sig, s2, d2);
+                            }
+                        }
+                    }
+                    S.rec[o[j].v].dlt = Prec::store(acc[j]);
+                    if (v != us[k].src) {
+                        const double card = us[k].card;
+                        const int64_t ov = sg.gid ? (int64_t)sg.gid[v] : sg.out_base + v;
+                        atomicAdd(P.bc + ov, card == 1.0 ? Prec::value(acc[j]) : card * Prec::value(acc[j]));
+                    }
                 }
             }
             __syncthreads();
         }
     }
     if (tid == 0 && bad) {
-        if (bad == kErrRetry) request_retry(P, u, kErrRetry);  // recomputed with 64-bit counts
-        else atomicOr(P.err, bad);
+        for (int k = 0; k < K; ++k) {
+            if (us[k].src < 0) continue;
+            if (bad == kErrRetry) request_retry(P, us[k], kErrRetry);  // recomputed with 64-bit counts
+            else atomicOr(P.err, bad);
+        }
     }
-    if (P.dbg_dist) {
+    if (P.dbg_dist) {  // single-source debug runs: source 0 of the group
+        const int src = us[0].src;
         for (int v = tid; v < n; v += nth) {
-            const int d = dist_of(ldcg64(S.word + v));
+            const int d = dist_of(ldcg64(S.word + v * K));
             P.dbg_dist[v] = d != kInf ? d : -1;
-            P.dbg_sig[v] = d != kInf ? (v == src ? 1ull : __ldcg(S.sc + v) >> 16) : 0ull;
-            P.dbg_dlt[v] = d != kInf ? Prec::value(Prec::load(S.dlt[v])) : 0.0;
+            P.dbg_sig[v] = d != kInf ? (v == src ? 1ull : __ldcg(&S.rec[v * K].sc) >> 16) : 0ull;
+            P.dbg_dlt[v] = d != kInf ? Prec::value(Prec::load(S.rec[v * K].dlt)) : 0.0;
         }
     }
     __syncthreads();
     // restore: word = (inf, 0), sigma/counter = 0
-    for (int v = tid; v < n; v += nth) {
-        S.word[v] = (unsigned long long)(unsigned)kInf << 32;
-        S.sc[v] = 0ull;
+    for (int i = tid; i < nK; i += nth) {
+        S.word[i] = (unsigned long long)(unsigned)kInf << 32;
+        S.rec[i].sc = 0ull;
     }
     __syncthreads();
 }
 
 // kWide: 512-thread blocks for segments whose frontiers span many hundreds of vertices
-// (millions of vertices); otherwise 128-thread blocks, five per SM.
-template <class Prec, bool kWide>
+// (millions of vertices); otherwise 128-thread blocks, five per SM.  K: sources per block;
+// units come in groups of K of one segment (padded with src = -1), P.nunits counts groups.
+template <class Prec, bool kWide, int K>
 __global__ void __launch_bounds__(kWide ? 512 : 128, kWide ? 1 : 5) frontier_kernel(KParams P) {
     __shared__ FCtl C;
+    __shared__ Unit us[K];
     char* slot = P.ws + (int64_t)blockIdx.x * P.ws_stride;
     unsigned* hdr = (unsigned*)slot;
-    FState<Prec> S = fstate_carve<Prec>(slot + 256, P.ws_n);
+    const int64_t cap = P.ws_n;  // entries of the slot (its layout depends on nothing else)
+    FState<Prec> S = fstate_carve<Prec>(slot + 256, cap);
     if (hdr[0] == 0u) {  // fresh slot: establish the between-units invariant
-        for (int i = threadIdx.x; i < P.ws_n; i += blockDim.x) {
+        for (int64_t i = threadIdx.x; i < cap; i += blockDim.x) {
             S.word[i] = (unsigned long long)(unsigned)kInf << 32;
-            S.sc[i] = 0ull;
+            S.rec[i].sc = 0ull;
         }
         __syncthreads();
         if (threadIdx.x == 0) hdr[0] = 1u;
@@ -490,10 +593,11 @@ __global__ void __launch_bounds__(kWide ? 512 : 128, kWide ? 1 : 5) frontier_ker
     for (;;) {
         if (threadIdx.x == 0) C.unit = (int)atomicAdd(P.next_unit, 1ull);
         __syncthreads();
-        const int64_t ui = C.unit;
+        const int64_t gi = C.unit;
+        if (gi < P.nunits && threadIdx.x < K) us[threadIdx.x] = P.units[gi * K + threadIdx.x];
         __syncthreads();
-        if (ui >= P.nunits) break;
-        frontier_unit<Prec>(P, ui, P.units[ui], S, C, P.ws_n);
+        if (gi >= P.nunits) break;
+        frontier_group<Prec, kWide ? 4 : 1, K>(P, us, S, C, cap);
     }
 }
 

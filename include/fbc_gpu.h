@@ -68,6 +68,8 @@ typedef struct {
                                 segment of n vertices and m edges counts 40*m + 52*n bytes  */
     int64_t warp_units;
     int64_t block_units;
+    int32_t group;           /* sources per block of the frontier kernel (0: not launched)  */
+    int32_t pad;
 } fbc_stats;
 
 /* Library lifetime.  fbc_gpu_init selects the device and creates the library stream. */
@@ -76,8 +78,9 @@ int fbc_gpu_shutdown(void);
 const char* fbc_last_error_string(void);
 
 /* Tuning knobs (the autotuner sets these): "delta" bucket width (0 = automatic),
- * "block_threads", "warp_max_n" (largest segment run warp-per-source), "iter_mult",
- * "ws_budget_mb".  Unknown key -> FBC_ERR_INVALID_ARG. */
+ * "block_threads", "frontier_threads", "group" (sources per block of the frontier kernel:
+ * 1, 2, 4, or 0 = automatic), "chunk_max", "wide_n", "warp_max_n" (largest segment run
+ * warp-per-source), "iter_mult", "ws_budget_mb".  Unknown key -> FBC_ERR_INVALID_ARG. */
 int fbc_set_option(const char* key, int64_t value);
 int fbc_get_option(const char* key, int64_t* value);
 

@@ -11,6 +11,7 @@
 //             replays ClusteredBrandeBC::computeBC step by step (ClusteredBrandesBC.h:63-169),
 //             dumping the partition, borders, pivots and cardinalities, the intra-cluster
 //             BC and the final BC, and also runs computeBC itself to cross-check the replay.
+//   partition <edges> <seeds> <prec> <out>          LouvainGraphPartition alone: the communities
 //   pins                                            the reference unit-test scenarios on DWGtext
 #define FASTBC_BRANDES_ENABLE_PIVOT_BORDER
 #define FASTBC_BRANDES_CLUSTERED_IGNORE_UNCONNECTED
@@ -95,6 +96,28 @@ int main(int argc, char** argv) {
             auto& x = vi[v];
             for (int i = 0; i < x->borders(); ++i)
                 std::fprintf(f, "%.17g %d ", x->getBorderSPLength(i), x->getBorderSPCount(i));
+            std::fprintf(f, "\n");
+        }
+        std::fclose(f);
+        return 0;
+    }
+    if (mode == "partition" && argc == 6) {
+        // LouvainGraphPartition::partitionGraph alone (ClusteredBrandesBC.h:75-76): one line per
+        // community, its vertices in the reference's order.
+        auto g = load(argv[2]);
+        std::set<std::mt19937::result_type> seeds;
+        {
+            std::stringstream ss(argv[3]);
+            std::mt19937::result_type s;
+            while (ss >> s) { seeds.insert(s); if (ss.peek() == ',') ss.ignore(); }
+        }
+        auto gp = std::make_shared<fastbc::louvain::LouvainGraphPartition<V, W>>(seeds, std::atof(argv[4]));
+        auto comms = gp->partitionGraph(std::static_pointer_cast<const fastbc::IDegreeGraph<V, W>>(g));
+        FILE* f = std::fopen(argv[5], "w");
+        std::fprintf(f, "%zu\n", comms.size());
+        for (const auto& c : comms) {
+            std::fprintf(f, "%zu", c.size());
+            for (V v : c) std::fprintf(f, " %d", v);
             std::fprintf(f, "\n");
         }
         std::fclose(f);

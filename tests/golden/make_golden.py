@@ -8,8 +8,12 @@ oracle/_ref/ref_harness) single-threaded on the seeded workloads and stores:
                              precision 0.01, kfrac 0.5): partition, borders, pivots and
                              cardinalities, intra-cluster BC, final BC (step replay and the
                              reference's own ClusteredBrandeBC::computeBC)
+  grid2048_partition.npz     LouvainGraphPartition (seeds 1-4, precision 0.01) of the
+                             2048x2048 grid: community id per vertex (int16; every
+                             community's vertices are ascending, as the reference lists them)
   DWGtext.txt                the reference unit tests' 9-vertex fixture (copied)
-The clustered run takes about 15 minutes on one core.  Usage:
+The clustered run takes about 15 minutes on one core, the 2048x2048 partition about a
+minute on eight.  Usage:
   python tests/golden/make_golden.py [--reuse DIR]   (DIR: outputs of an earlier harness run)
 """
 from __future__ import annotations
@@ -89,6 +93,22 @@ def main():
                         cluster_vertices=cv, border_off=boff, borders=bv, pivot_off=poff,
                         pivots=pv, cards=kv, intra_bc=np.loadtxt(pre + ".intra"), bc=bc_ref,
                         bc_replay=bc)
+    g2048 = os.path.join(work, "grid2048.txt")
+    if not os.path.exists(g2048):
+        graphs.WORKLOADS["grid2048"]().write(g2048)
+    part = os.path.join(work, "grid2048.part")
+    if not os.path.exists(part):
+        subprocess.run([HARNESS, "partition", g2048, "1,2,3,4", "0.01", part], check=True,
+                       env=dict(os.environ, OMP_NUM_THREADS="8"))
+    with open(part) as f:
+        lines = f.read().split("\n")
+    comms = [np.array(lines[1 + i].split()[1:], np.int32) for i in range(int(lines[0]))]
+    cid = np.full(sum(c.size for c in comms), -1, np.int16)
+    for i, c in enumerate(comms):
+        assert np.all(np.diff(c) > 0)
+        cid[c] = i
+    assert np.all(cid >= 0)
+    np.savez_compressed(os.path.join(HERE, "grid2048_partition.npz"), community=cid)
     print("golden fixtures written to", HERE)
 
 
