@@ -307,7 +307,7 @@ __device__ void small_unit(const KParams& K, const Seg& sg, const Unit& u, const
                 dlt[v] = Prec::store(acc);
                 if (v != src) {
                     const double c = card == 1.0 ? Prec::value(acc) : card * Prec::value(acc);
-                    atomicAdd(K.bc + (sg.gid ? (int64_t)sg.gid[v] : sg.out_base + v), c);
+                    atomicAdd(K.bc + sg.out_base + (sg.gid ? sg.gid[v] : v), c);
                 }
             }
             __syncwarp();

@@ -46,7 +46,7 @@ enum : int { kErrIter = 1, kErrSigma = 2, kErrQueue = 4, kErrRetry = 8 };
 struct Seg {
     const int32_t* rp;      // n+1 row offsets into adj
     const int2* adj;        // packed (destination, weight) pairs, rows ascending
-    const int32_t* gid;     // n output indices (local -> BC index); null: out_base + local id
+    const int32_t* gid;     // n local -> output ids; BC index = out_base + (gid ? gid[v] : v)
     const int32_t* border;  // nb local ids of the border vertices (ascending global id)
     int64_t out_base;
     int32_t n;              // vertices
@@ -580,7 +580,7 @@ __device__ void run_unit(const KParams& P, const Unit& u, const State<Prec>& S, 
                 }
                 S.dlt[v] = Prec::store(acc);
                 if (v != src) {
-                    const int64_t o = gid ? (int64_t)gid[v] : sg.out_base + v;
+                    const int64_t o = sg.out_base + (gid ? gid[v] : v);
                     atomicAdd(P.bc + o, card * Prec::value(acc));
                 }
             }

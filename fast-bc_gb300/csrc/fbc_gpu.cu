@@ -49,7 +49,9 @@ int fail(int code, const std::string& msg) {
 struct DBuf {
     void* p = nullptr;
     size_t cap = 0;
-    cudaError_t ensure(size_t bytes, bool zero = false) {
+    // zero: clear a new allocation on `zst`, the stream its first user runs on (a plain
+    // cudaMemset would run on the legacy stream, unordered with a non-blocking stream)
+    cudaError_t ensure(size_t bytes, bool zero = false, cudaStream_t zst = nullptr) {
         if (p && bytes <= cap) return cudaSuccess;
         if (p) cudaFree(p);
         p = nullptr;
@@ -61,7 +63,7 @@ struct DBuf {
             return e;
         }
         cap = want;
-        if (zero) return cudaMemset(p, 0, want);
+        if (zero) return cudaMemsetAsync(p, 0, want, zst);
         return cudaSuccess;
     }
     void release() {
@@ -85,6 +87,7 @@ struct Options {
     int64_t iter_mult = 16;
     int64_t ws_budget_mb = 0;   // 0 = 60% of the free device memory
     int64_t group = 0;          // frontier kernel sources per block (1, 2, 4); 0 = automatic
+    int64_t order_min_n = 131072;  // batched runs relabel graphs of at least this many vertices
     int64_t warp_smem = 1;      // batched: warp state in shared memory when it fits
     int64_t debug_sched = FBC_SCHED_PLAIN;  // schedule used by fbc_sssp_debug
 };
@@ -131,6 +134,13 @@ struct fbc_graph_s {
     std::vector<int64_t> h_rp;
     std::vector<int32_t> h_col;
     std::vector<int32_t> h_w;
+    // locality order for the batched schedule, built on first use: the CSR relabelled by
+    // recursive BFS bisection (ord_new: input id -> new id; d_ord_inv: new id -> input id)
+    bool ord_built = false;
+    int32_t* d_ord_rp = nullptr;
+    int2* d_ord_adj = nullptr;
+    int32_t* d_ord_inv = nullptr;
+    std::vector<int32_t> ord_new;
 };
 
 struct fbc_plan_s {
@@ -247,6 +257,89 @@ struct Plan {
     double* dbg_dlt = nullptr;
 };
 
+// Recursive BFS bisection: a part (a range of `ord`) is laid out in the order of a BFS from its
+// first vertex that stays inside the part (vertices it cannot reach follow in their current
+// order), then halved; parts of at most `leaf` vertices are sorted by id.  Neighbours end up
+// close together at every scale, so a wavefront's vertices share sectors and DRAM pages.
+std::vector<int32_t> bisection_order(int32_t n, const std::vector<int64_t>& rp, const std::vector<int32_t>& col,
+                                     int leaf) {
+    std::vector<int32_t> ord((size_t)n), tmp((size_t)n), part((size_t)n, 0);
+    std::vector<char> vis((size_t)n, 0);
+    for (int32_t i = 0; i < n; ++i) ord[i] = i;
+    std::vector<std::pair<int64_t, int64_t>> stk;
+    stk.emplace_back(0, n);
+    int32_t pid = 1;
+    while (!stk.empty()) {
+        const auto [lo, hi] = stk.back();
+        stk.pop_back();
+        const int64_t len = hi - lo;
+        if (len <= leaf) {
+            std::sort(ord.begin() + lo, ord.begin() + hi);
+            continue;
+        }
+        const int32_t me = pid++;
+        for (int64_t i = lo; i < hi; ++i) part[ord[i]] = me;
+        int64_t qt = 0;
+        for (int64_t i = lo; i < hi; ++i) {
+            const int32_t s0 = ord[i];
+            if (vis[s0]) continue;
+            int64_t qh = qt;
+            tmp[qt++] = s0;
+            vis[s0] = 1;
+            while (qh < qt) {
+                const int32_t v = tmp[qh++];
+                for (int64_t e = rp[v]; e < rp[v + 1]; ++e) {
+                    const int32_t x = col[e];
+                    if (part[x] == me && !vis[x]) {
+                        vis[x] = 1;
+                        tmp[qt++] = x;
+                    }
+                }
+            }
+        }
+        for (int64_t i = 0; i < len; ++i) {
+            ord[lo + i] = tmp[i];
+            vis[tmp[i]] = 0;
+        }
+        const int64_t mid = lo + len / 2;
+        stk.emplace_back(mid, hi);
+        stk.emplace_back(lo, mid);
+    }
+    std::vector<int32_t> nw((size_t)n);
+    for (int32_t i = 0; i < n; ++i) nw[ord[i]] = i;
+    return nw;
+}
+
+// Build (once) the relabelled device CSR of a graph: rows ascending in the new ids.
+int ensure_order(fbc_graph_s* G) {
+    if (G->ord_built) return FBC_OK;
+    const int32_t n = G->n;
+    std::vector<int32_t> nw = bisection_order(n, G->h_rp, G->h_col, 16);
+    std::vector<int32_t> inv((size_t)std::max(n, 1));
+    for (int32_t v = 0; v < n; ++v) inv[nw[v]] = v;
+    std::vector<int32_t> rp32((size_t)n + 1, 0);
+    std::vector<int2> adj((size_t)std::max<int64_t>(G->m, 1));
+    int64_t e = 0;
+    for (int32_t u = 0; u < n; ++u) {
+        const int32_t v = inv[u];
+        rp32[u] = (int32_t)e;
+        const int64_t b = e;
+        for (int64_t k = G->h_rp[v]; k < G->h_rp[v + 1]; ++k) adj[e++] = make_int2(nw[G->h_col[k]], G->h_w[k]);
+        std::sort(adj.begin() + b, adj.begin() + e, [](const int2& a, const int2& c) { return a.x < c.x; });
+    }
+    rp32[n] = (int32_t)e;
+    FBC_CK(cudaMalloc(&G->d_ord_rp, sizeof(int32_t) * rp32.size()));
+    FBC_CK(cudaMalloc(&G->d_ord_adj, sizeof(int2) * adj.size()));
+    FBC_CK(cudaMalloc(&G->d_ord_inv, sizeof(int32_t) * inv.size()));
+    FBC_CK(cudaMemcpyAsync(G->d_ord_rp, rp32.data(), sizeof(int32_t) * rp32.size(), cudaMemcpyHostToDevice, g.st));
+    FBC_CK(cudaMemcpyAsync(G->d_ord_adj, adj.data(), sizeof(int2) * adj.size(), cudaMemcpyHostToDevice, g.st));
+    FBC_CK(cudaMemcpyAsync(G->d_ord_inv, inv.data(), sizeof(int32_t) * inv.size(), cudaMemcpyHostToDevice, g.st));
+    FBC_CK(cudaStreamSynchronize(g.st));
+    G->ord_new = std::move(nw);
+    G->ord_built = true;
+    return FBC_OK;
+}
+
 Seg whole_graph_seg(const fbc_graph_s* G, int64_t out_base) {
     Seg s{};
     s.rp = G->d_rp;
@@ -282,7 +375,7 @@ KParams base_params(const Plan& P) {
 int ensure_ws(Workspace& W, int64_t slots, int64_t stride, int ws_n, int dsize) {
     if (W.buf.p && W.ws_n >= ws_n && W.dsize == dsize && W.slots >= slots) return FBC_OK;
     W.buf.release();
-    FBC_CK(W.buf.ensure((size_t)(slots * stride), true));
+    FBC_CK(W.buf.ensure((size_t)(slots * stride), true, g.st));
     W.stride = stride;
     W.slots = slots;
     W.ws_n = ws_n;
@@ -867,6 +960,7 @@ int fbc_set_option(const char* key, int64_t value) {
     else if (k == "warp_max_n") g.opt.warp_max_n = std::max<int64_t>(0, value);
     else if (k == "iter_mult") g.opt.iter_mult = std::max<int64_t>(1, std::min<int64_t>(1 << 20, value));
     else if (k == "ws_budget_mb") g.opt.ws_budget_mb = std::max<int64_t>(0, value);
+    else if (k == "order_min_n") g.opt.order_min_n = std::max<int64_t>(0, value);
     else if (k == "group") {
         if (value != 0 && value != 1 && value != 2 && value != 4) return fail(FBC_ERR_INVALID_ARG, "group must be 0, 1, 2 or 4");
         g.opt.group = value;
@@ -890,6 +984,7 @@ int fbc_get_option(const char* key, int64_t* value) {
     else if (k == "iter_mult") *value = g.opt.iter_mult;
     else if (k == "ws_budget_mb") *value = g.opt.ws_budget_mb;
     else if (k == "group") *value = g.opt.group;
+    else if (k == "order_min_n") *value = g.opt.order_min_n;
     else if (k == "warp_smem") *value = g.opt.warp_smem;
     else if (k == "debug_sched") *value = g.opt.debug_sched;
     else return fail(FBC_ERR_INVALID_ARG, "unknown option " + k);
@@ -970,12 +1065,30 @@ int fbc_graph_download(fbc_graph G, int64_t* row_ptr, int32_t* col, double* w) {
     return FBC_OK;
 }
 
+// The whole-graph segment a batched run uses: graphs of at least `order_min_n` vertices run on
+// their relabelled CSR (outputs go back to input ids through gid); `map` then translates source
+// ids.  Plain runs and debug dumps use the input order.
+int batched_graph_seg(fbc_graph_s* G, int64_t out_base, int sched, Seg& s, const int32_t*& map) {
+    s = whole_graph_seg(G, out_base);
+    map = nullptr;
+    if (sched != FBC_SCHED_BATCHED || (int64_t)G->n < g.opt.order_min_n) return FBC_OK;
+    FBC_TRY(ensure_order(G));
+    s.rp = G->d_ord_rp;
+    s.adj = G->d_ord_adj;
+    s.gid = G->d_ord_inv;
+    map = G->ord_new.data();
+    return FBC_OK;
+}
+
 int fbc_graph_free(fbc_graph G) {
     std::lock_guard<std::recursive_mutex> lk(g_mu);
     if (!G) return FBC_OK;
     if (g.init) cudaStreamSynchronize(g.st);
     cudaFree(G->d_rp);
     cudaFree(G->d_adj);
+    if (G->d_ord_rp) cudaFree(G->d_ord_rp);
+    if (G->d_ord_adj) cudaFree(G->d_ord_adj);
+    if (G->d_ord_inv) cudaFree(G->d_ord_inv);
     delete G;
     return FBC_OK;
 }
@@ -990,7 +1103,10 @@ int fbc_exact_bc(fbc_graph G, int precision, int sched, double* out_bc, fbc_stat
     Plan P;
     P.prec = precision;
     P.sched = sched;
-    P.segs.push_back(whole_graph_seg(G, 0));
+    Seg sg;
+    const int32_t* map = nullptr;
+    FBC_TRY(batched_graph_seg(G, 0, sched, sg, map));
+    P.segs.push_back(sg);
     P.seg_m.push_back(G->m);
     P.seg_maxw.push_back(G->maxw);
     P.seg_maxindeg.push_back(G->maxindeg);
@@ -1015,14 +1131,17 @@ int fbc_sssp_dependency_batch(fbc_graph G, int64_t count, const int32_t* sources
     Plan P;
     P.prec = precision;
     P.sched = sched;
-    P.segs.push_back(whole_graph_seg(G, 0));
+    for (int64_t i = 0; i < count; ++i)
+        if (sources[i] < 0 || sources[i] >= G->n) return fail(FBC_ERR_INVALID_ARG, "source out of range");
+    Seg sg;
+    const int32_t* map = nullptr;
+    FBC_TRY(batched_graph_seg(G, 0, sched, sg, map));
+    P.segs.push_back(sg);
     P.seg_m.push_back(G->m);
     P.seg_maxw.push_back(G->maxw);
     P.seg_maxindeg.push_back(G->maxindeg);
-    for (int64_t i = 0; i < count; ++i) {
-        if (sources[i] < 0 || sources[i] >= G->n) return fail(FBC_ERR_INVALID_ARG, "source out of range");
-        P.units.push_back(Unit{0, sources[i], cards ? cards[i] : 1.0, -1});
-    }
+    for (int64_t i = 0; i < count; ++i)
+        P.units.push_back(Unit{0, map ? map[sources[i]] : sources[i], cards ? cards[i] : 1.0, -1});
     P.bc_len = G->n;
     if (st) st->h2d_bytes += count * (int64_t)(sizeof(int32_t) + sizeof(double));
     FBC_TRY(run_plan(P, st));
@@ -1284,7 +1403,10 @@ int fbc_multi_exact_bc(int32_t ngraphs, const fbc_graph* graphs, int precision, 
     std::vector<int64_t> base((size_t)ngraphs + 1, 0);
     for (int32_t i = 0; i < ngraphs; ++i) {
         if (!graphs[i]) return fail(FBC_ERR_INVALID_ARG, "null graph in batch");
-        P.segs.push_back(whole_graph_seg(graphs[i], base[i]));
+        Seg sg;
+        const int32_t* map = nullptr;
+        FBC_TRY(batched_graph_seg(graphs[i], base[i], sched, sg, map));
+        P.segs.push_back(sg);
         P.seg_m.push_back(graphs[i]->m);
         P.seg_maxw.push_back(graphs[i]->maxw);
         P.seg_maxindeg.push_back(graphs[i]->maxindeg);

@@ -143,8 +143,10 @@ __device__ __forceinline__ void bpush(bool want, const E& x, E* q, int* c, int c
 // words of nearby sources' wavefronts share sectors and the adjacency rows they read are the
 // same.  Queue and level entries name an entry vk = v*K + k.  K = 1 is one source per block.
 // kV: vertices per lane in the Kahn and dependency passes (4 for the wide blocks of
-// million-vertex graphs, whose levels are thousands wide; 1 for the narrow blocks).
-template <class Prec, int kV, int K>
+// million-vertex graphs, whose levels are thousands wide; 1 for the narrow blocks); kE:
+// queued entries per lane in the distance pass (1: two measured slower on the wide blocks,
+// which then spill at their 128-register cap).
+template <class Prec, int kV, int K, int kE>
 __device__ void frontier_group(const KParams& P, const Unit* us, const FState<Prec>& S, FCtl& C,
                                int64_t cap) {
     static_assert(K == 1 || K == 2 || K == 4 || K == 8, "K is a power of two up to 8");
@@ -190,51 +192,63 @@ __device__ void frontier_group(const KParams& P, const Unit* us, const FState<Pr
             const QEnt* qc = qs ? S.q[1] : S.q[0];
             QEnt* qnx = qs ? S.q[0] : S.q[1];
             QEnt* qfx = fs ? S.q[3] : S.q[2];
-            // warp-uniform trip count so that every lane reaches the ballots
-            for (int base = tid & ~31; base < ncur; base += nth) {
-                const int i = base + (tid & 31);
-                int e = 0, e1 = 0, dv = 0, k = 0;
-                if (i < ncur) {
-                    const QEnt q = qc[i];
-                    e = q.e0;
-                    e1 = q.e0 + q.deg;
-                    k = q.v & (K - 1);
-                    dv = dist_of(ldcg64(S.word + q.v));  // may have dropped since the push
-                }
-                while (__any_sync(kFull, e < e1)) {
-                    int x[4], nd[4], r0[4], r1[4];
-                    unsigned long long old[4];
+            // warp-uniform trip count so that every lane reaches the ballots; each lane takes
+            // kE queued entries (entries j*32 + lane of the warp's span) and issues up to four
+            // edges of each at once
+            for (int base = (tid & ~31) * kE; base < ncur; base += nth * kE) {
+                int e[kE], e1[kE], dv[kE], kk[kE];
 #pragma unroll
-                    for (int j = 0; j < 4; ++j) {
-                        x[j] = -1;
-                        if (e + j < e1) {
-                            const int4 a = __ldg(adjx + e + j);  // (x, w, x's row start, x's degree)
-                            x[j] = (a.x << kSh) + k;
-                            nd[j] = dv + a.y;
-                            r0[j] = a.z;
-                            r1[j] = a.z + a.w;
+                for (int j = 0; j < kE; ++j) {
+                    const int i = base + j * 32 + (tid & 31);
+                    e[j] = e1[j] = dv[j] = kk[j] = 0;
+                    if (i < ncur) {
+                        const QEnt q = qc[i];
+                        e[j] = q.e0;
+                        e1[j] = q.e0 + q.deg;
+                        kk[j] = q.v & (K - 1);
+                        dv[j] = dist_of(ldcg64(S.word + q.v));  // may have dropped since the push
+                    }
+                }
+                for (;;) {
+                    bool more = false;
+#pragma unroll
+                    for (int j = 0; j < kE; ++j) more |= e[j] < e1[j];
+                    if (!__any_sync(kFull, more)) break;
+                    int x[kE * 4], nd[kE * 4], r0[kE * 4], r1[kE * 4];
+                    unsigned long long old[kE * 4];
+#pragma unroll
+                    for (int t = 0; t < kE * 4; ++t) {
+                        const int j = t / 4, q = t % 4;
+                        x[t] = -1;
+                        if (e[j] + q < e1[j]) {
+                            const int4 a = __ldg(adjx + e[j] + q);  // (x, w, x's row start, x's degree)
+                            x[t] = (a.x << kSh) + kk[j];
+                            nd[t] = dv[j] + a.y;
+                            r0[t] = a.z;
+                            r1[t] = a.z + a.w;
                         }
                     }
 #pragma unroll
-                    for (int j = 0; j < 4; ++j)
-                        if (x[j] >= 0)
-                            old[j] = atomicMin(S.word + x[j],
-                                               ((unsigned long long)(unsigned)nd[j] << 32) | (nd[j] < T ? nst : fst));
+                    for (int t = 0; t < kE * 4; ++t)
+                        if (x[t] >= 0)
+                            old[t] = atomicMin(S.word + x[t],
+                                               ((unsigned long long)(unsigned)nd[t] << 32) | (nd[t] < T ? nst : fst));
 #pragma unroll
-                    for (int j = 0; j < 4; ++j) {
+                    for (int t = 0; t < kE * 4; ++t) {
                         bool pn = false, pf = false;
-                        if (x[j] >= 0) {
-                            const bool near = nd[j] < T;
-                            if (nd[j] < dist_of(old[j]) && (unsigned)old[j] != (near ? nst : fst)) {
+                        if (x[t] >= 0) {
+                            const bool near = nd[t] < T;
+                            if (nd[t] < dist_of(old[t]) && (unsigned)old[t] != (near ? nst : fst)) {
                                 pn = near;
                                 pf = !near;
                             }
                         }
-                        const QEnt qe{x[j], r0[j], r1[j] - r0[j], 0};
+                        const QEnt qe{x[t], r0[t], r1[t] - r0[t], 0};
                         bpush(pn, qe, qnx, &C.ncnt[qs ^ 1], qc_cap, &C.ovf);
                         bpush(pf, qe, qfx, &C.fcnt[fs], qc_cap, &C.ovf);
                     }
-                    e += 4;
+#pragma unroll
+                    for (int j = 0; j < kE; ++j) e[j] += 4;
                 }
             }
             __syncthreads();
@@ -538,7 +552,7 @@ __device__ void frontier_group(const KParams& P, const Unit* us, const FState<Pr
                     S.rec[o[j].v].dlt = Prec::store(acc[j]);
                     if (v != us[k].src) {
                         const double card = us[k].card;
-                        const int64_t ov = sg.gid ? (int64_t)sg.gid[v] : sg.out_base + v;
+                        const int64_t ov = sg.out_base + (sg.gid ? sg.gid[v] : v);
                         atomicAdd(P.bc + ov, card == 1.0 ? Prec::value(acc[j]) : card * Prec::value(acc[j]));
                     }
                 }
@@ -597,7 +611,7 @@ __global__ void __launch_bounds__(kWide ? 512 : 128, kWide ? 1 : 5) frontier_ker
         if (gi < P.nunits && threadIdx.x < K) us[threadIdx.x] = P.units[gi * K + threadIdx.x];
         __syncthreads();
         if (gi >= P.nunits) break;
-        frontier_group<Prec, kWide ? 4 : 1, K>(P, us, S, C, cap);
+        frontier_group<Prec, kWide ? 4 : 1, K, 1>(P, us, S, C, cap);
     }
 }
 
