@@ -53,8 +53,6 @@ struct Seg {
     int32_t nb;             // border vertices (cluster segments), else 0
     int32_t delta;          // bucket width of the near-far pass
     int32_t pad;
-    const int4* adjx;       // frontier kernel: adj with each destination's row start and
-                            // degree, (x, w, rp[x], rp[x+1] - rp[x])
 };
 
 // One source.

@@ -110,7 +110,7 @@ struct Ctx {
     cudaStream_t st = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, evm = nullptr;
     Options opt;
-    DBuf retry, segs, units_b, units_w, chunks, crp, cadj, cgid, cbord, bc, bdist, bsig, ctr, dbg, adjx;
+    DBuf retry, segs, units_b, units_w, chunks, crp, cadj, cgid, cbord, bc, bdist, bsig, ctr, dbg;
     Workspace wsb, wsw;
 };
 Ctx g;
@@ -652,28 +652,6 @@ int run_plan_t(Plan& P, fbc_stats* st) {
                 P.sched = FBC_SCHED_PLAIN;
                 break;
             }
-    // the frontier kernel reads each segment's annotated adjacency
-    if (P.sched == FBC_SCHED_BATCHED && !ub.empty()) {
-        std::vector<int64_t> xoff(P.segs.size(), -1);
-        int64_t tot = 0;
-        for (const Unit& u : ub)
-            if (xoff[u.seg] < 0) {
-                xoff[u.seg] = tot;
-                tot += P.seg_m[u.seg];
-            }
-        FBC_CK(g.adjx.ensure(sizeof(int4) * (size_t)std::max<int64_t>(tot, 1)));
-        for (size_t s = 0; s < P.segs.size(); ++s)
-            if (xoff[s] >= 0) {
-                int4* dst = g.adjx.as<int4>() + xoff[s];
-                if (P.seg_m[s] > 0) {
-                    const int64_t blocks = std::min<int64_t>((P.seg_m[s] + 255) / 256, (int64_t)g.nsm * 8);
-                    fbc::build_adjx_kernel<<<(unsigned)blocks, 256, 0, g.st>>>(P.segs[s].rp, P.segs[s].adj,
-                                                                             P.seg_m[s], dst);
-                    FBC_CK(cudaGetLastError());
-                }
-                P.segs[s].adjx = dst;
-            }
-    }
     FBC_CK(g.segs.ensure(sizeof(Seg) * std::max<size_t>(P.segs.size(), 1)));
     FBC_CK(cudaMemcpyAsync(g.segs.p, P.segs.data(), sizeof(Seg) * P.segs.size(),
                            cudaMemcpyHostToDevice, g.st));
@@ -933,7 +911,7 @@ int fbc_gpu_shutdown(void) {
     std::lock_guard<std::recursive_mutex> lk(g_mu);
     if (!g.init) return FBC_OK;
     cudaStreamSynchronize(g.st);
-    for (DBuf* b : {&g.adjx, &g.retry, &g.segs, &g.units_b, &g.units_w, &g.chunks, &g.crp, &g.cadj, &g.cgid, &g.cbord, &g.bc,
+    for (DBuf* b : {&g.retry, &g.segs, &g.units_b, &g.units_w, &g.chunks, &g.crp, &g.cadj, &g.cgid, &g.cbord, &g.bc,
                     &g.bdist, &g.bsig, &g.ctr, &g.dbg})
         b->release();
     g.wsb.buf.release();

@@ -1,17 +1,23 @@
 // Batched schedule, large segments (whole graphs: pivots, exact mode, big graphs of a
-// batch): one source per thread block, per-source state in a global-memory slot, blocks
-// pulling units from a shared counter.  Same passes and predecessor rule as
-// brandes_kernels.cuh; what shortens each step's chain of dependent memory accesses:
+// batch): one source (or a group of K sources) per thread block, per-source state in a
+// global-memory slot, blocks pulling units from a shared counter.  Same passes and predecessor
+// rule as brandes_kernels.cuh.  On million-vertex graphs the kernel is bound by random DRAM
+// sector accesses (every vertex's state and row is touched cold once per pass), so the
+// design counts sectors and dependent steps:
 //   * one 64-bit word per vertex, (dist << 32 | stamp): a single global atomicMin both relaxes
 //     the edge and reports whether the vertex already sits in the queue the relaxation
 //     pushes it to (the queue's stamp), so there is no second atomic on a flag array;
-//   * queue entries carry the vertex's row (loaded alongside the atomic that pushed it) and
-//     Kahn-level entries carry distance, row and final path count, so a step starts with
-//     its adjacency loads; path count and the Kahn counter share one 64-bit word
-//     (sigma << 16 | counter), so one atomic both adds sigma_v and retires the edge, and the
-//     thread that retires the last tight in-edge learns the final count;
-//   * each thread takes one queued vertex and issues up to four of its edges at once, so
-//     their loads and atomics are in flight together (road-like graphs: degree <= ~6);
+//   * queue entries carry the vertex's row (loaded from the small, L2-resident row offsets
+//     alongside the atomic that pushed it) and Kahn-level entries carry distance, row, final
+//     path count and tight-edge mask, so a step starts with its adjacency loads;
+//   * path count and Kahn counter share one 64-bit word (sigma << 16 | counter), so one atomic
+//     both adds sigma_v and retires the edge, and the thread that retires the last tight
+//     in-edge learns the final count; the word sits in a 16-byte record with the dependency
+//     (which holds the tight-edge mask until the dependency pass), so a Kahn push and a
+//     dependency pull each touch one sector of the pushed/pulled vertex;
+//   * each thread takes one queued vertex and issues up to four of its edges at once (and
+//     one or two level entries at once in the Kahn and dependency passes), so their loads
+//     and atomics are in flight together;
 //   * sigma_v == sigma_w takes the exact ratio-1 path in the dependency pass.
 #pragma once
 #include "batched_kernels.cuh"
@@ -42,11 +48,16 @@ __host__ __device__ inline int64_t fqcap(int64_t cap) {
 }
 
 // Path count and dependency of a vertex side by side, so the dependency pass reads both with
-// one 16-byte load.
+// one 16-byte load.  Until the dependency pass writes it, the dependency slot holds the
+// vertex's tight out-edge mask (bit k: edge e0 + k; all ones for rows longer than 32 edges),
+// so the Kahn pass finds a released vertex's mask in the sector its count atomic just touched.
 template <class Prec>
 struct __align__(16) FRec {
     unsigned long long sc;        // (sigma << 16 | tight in-edges still unprocessed)
-    typename Prec::D dlt;
+    union {
+        typename Prec::D dlt;
+        unsigned mask;
+    };
 };
 
 template <class Prec>
@@ -56,14 +67,13 @@ struct FState {
     QEnt* q[4];                   // near0, near1, far0, far1 (fqcap(cap) entries)
     LEnt* order;                  // cap + 1 entries
     int* lvl;                     // cap + 1 entries
-    unsigned* tmask;              // tight out-edge mask per vertex (cap entries)
 };
 
 template <class Prec>
 __host__ __device__ inline int64_t fstate_bytes(int64_t cap) {
     auto al = [](int64_t x) { return (x + 255) & ~int64_t(255); };
     return al(cap * 8) + al(cap * (int64_t)sizeof(FRec<Prec>)) + 4 * al(fqcap(cap) * (int64_t)sizeof(QEnt)) + al((cap + 1) * (int64_t)sizeof(LEnt)) +
-           al((cap + 1) * 4) + al(cap * 4);
+           al((cap + 1) * 4);
 }
 
 template <class Prec>
@@ -74,8 +84,7 @@ __device__ inline FState<Prec> fstate_carve(char* p, int64_t cap) {
     s.rec = (FRec<Prec>*)p; p += al(cap * (int64_t)sizeof(FRec<Prec>));
     for (int i = 0; i < 4; ++i) { s.q[i] = (QEnt*)p; p += al(fqcap(cap) * (int64_t)sizeof(QEnt)); }
     s.order = (LEnt*)p; p += al((cap + 1) * (int64_t)sizeof(LEnt));
-    s.lvl = (int*)p; p += al((cap + 1) * 4);
-    s.tmask = (unsigned*)p;
+    s.lvl = (int*)p;
     return s;
 }
 
@@ -107,16 +116,6 @@ __device__ __forceinline__ float2 bits_to<float2>(unsigned long long b) {
     return make_float2(__int_as_float((int)(unsigned)b), __int_as_float((int)(unsigned)(b >> 32)));
 }
 
-// Annotated adjacency of one segment: (x, w, rp[x], rp[x+1] - rp[x]) for every edge, so that a
-// relaxation that pushes x already holds x's row.
-__global__ void build_adjx_kernel(const int* __restrict__ rp, const int2* __restrict__ adj, int64_t m,
-                                  int4* __restrict__ out) {
-    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < m; e += (int64_t)gridDim.x * blockDim.x) {
-        const int2 a = adj[e];
-        const int r0 = __ldg(rp + a.x), r1 = __ldg(rp + a.x + 1);
-        out[e] = make_int4(a.x, a.y, r0, r1 - r0);
-    }
-}
 __device__ __forceinline__ int dist_of(unsigned long long w) { return (int)(w >> 32); }
 
 // Block-wide push (warp-aggregated slot reservation on a shared-memory counter); a push past
@@ -142,8 +141,9 @@ __device__ __forceinline__ void bpush(bool want, const E& x, E* q, int* c, int c
 // of them), and their per-vertex state is interleaved, entry v*K + k for source k, so the
 // words of nearby sources' wavefronts share sectors and the adjacency rows they read are the
 // same.  Queue and level entries name an entry vk = v*K + k.  K = 1 is one source per block.
-// kV: vertices per lane in the Kahn and dependency passes (4 for the wide blocks of
-// million-vertex graphs, whose levels are thousands wide; 1 for the narrow blocks); kE:
+// kV: vertices per lane in the Kahn and dependency passes (2 for the wide blocks of
+// million-vertex graphs, whose levels are thousands wide -- 4 measured slower, spilling at the
+// 128-register cap; 1 for the narrow blocks); kE:
 // queued entries per lane in the distance pass (1: two measured slower on the wide blocks,
 // which then spill at their 128-register cap).
 template <class Prec, int kV, int K, int kE>
@@ -156,7 +156,6 @@ __device__ void frontier_group(const KParams& P, const Unit* us, const FState<Pr
     const int nK = n * K;
     const int* __restrict__ rp = sg.rp;
     const int2* __restrict__ adj = sg.adj;
-    const int4* __restrict__ adjx = sg.adjx;
     const int delta = sg.delta > 0 ? sg.delta : 1;
     const int tid = threadIdx.x, nth = blockDim.x;
     const int qc_cap = (int)fqcap(cap);
@@ -221,11 +220,11 @@ __device__ void frontier_group(const KParams& P, const Unit* us, const FState<Pr
                         const int j = t / 4, q = t % 4;
                         x[t] = -1;
                         if (e[j] + q < e1[j]) {
-                            const int4 a = __ldg(adjx + e[j] + q);  // (x, w, x's row start, x's degree)
+                            const int2 a = __ldg(adj + e[j] + q);
                             x[t] = (a.x << kSh) + kk[j];
                             nd[t] = dv[j] + a.y;
-                            r0[t] = a.z;
-                            r1[t] = a.z + a.w;
+                            r0[t] = __ldg(rp + a.x);  // x's row, in flight with the atomic
+                            r1[t] = __ldg(rp + a.x + 1);
                         }
                     }
 #pragma unroll
@@ -353,7 +352,7 @@ __device__ void frontier_group(const KParams& P, const Unit* us, const FState<Pr
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
                 const int vk = v0 + j * nth;
-                if (vk < nK && dv[j] != kInf) S.tmask[vk] = e1[j] - eb[j] > 32 ? 0xffffffffu : mk[j];
+                if (vk < nK && dv[j] != kInf) S.rec[vk].mask = e1[j] - eb[j] > 32 ? 0xffffffffu : mk[j];
             }
         }
         __syncthreads();
@@ -362,7 +361,7 @@ __device__ void frontier_group(const KParams& P, const Unit* us, const FState<Pr
             for (int k = 0; k < K; ++k) {
                 const int src = us[k].src;
                 if (src < 0) continue;
-                S.order[c++] = LEnt{src * K + k, 0, __ldg(rp + src), __ldcg(S.tmask + src * K + k), 1ull};
+                S.order[c++] = LEnt{src * K + k, 0, __ldg(rp + src), __ldcg(&S.rec[src * K + k].mask), 1ull};
             }
             S.lvl[0] = 0;
             C.ocnt = c;
@@ -419,10 +418,10 @@ __device__ void frontier_group(const KParams& P, const Unit* us, const FState<Pr
                             ei = e[j]++;
                         }
                         if (ei >= 0) {
-                            const int4 a = __ldg(adjx + ei);  // x's row start comes along
+                            const int2 a = __ldg(adj + ei);
                             x[j] = (a.x << kSh) + kk[j];
                             nd[j] = dv[j] + a.y;
-                            r0[j] = a.z;
+                            r0[j] = __ldg(rp + a.x);  // row offsets: small and shared, L2-resident
                         }
                     }
 #pragma unroll
@@ -436,7 +435,7 @@ __device__ void frontier_group(const KParams& P, const Unit* us, const FState<Pr
                             // one atomic adds sigma_v and retires the edge; the thread that
                             // retires the last tight in-edge knows x's final count
                             old[j] = atomicAdd(&S.rec[x[j]].sc, (sv[j] << 16) - 1ull);
-                            tm[j] = __ldcg(S.tmask + x[j]);  // in flight with the atomic
+                            tm[j] = __ldcg(&S.rec[x[j]].mask);  // same sector as the atomic
                         }
 #pragma unroll
                     for (int j = 0; j < kV; ++j) {
@@ -611,7 +610,7 @@ __global__ void __launch_bounds__(kWide ? 512 : 128, kWide ? 1 : 5) frontier_ker
         if (gi < P.nunits && threadIdx.x < K) us[threadIdx.x] = P.units[gi * K + threadIdx.x];
         __syncthreads();
         if (gi >= P.nunits) break;
-        frontier_group<Prec, kWide ? 4 : 1, K, 1>(P, us, S, C, cap);
+        frontier_group<Prec, kWide ? 2 : 1, K, 1>(P, us, S, C, cap);
     }
 }
 
