@@ -221,6 +221,8 @@ class GridClustered4M(Workload):
         allp = np.concatenate([piv[c] for c in nonempty])
         allc = np.concatenate([cards[c] for c in nonempty])
         sel = np.arange(0, allp.size, step)
+        if args.max_pivots > 0:
+            sel = sel[: args.max_pivots]
         self.pv, self.kv = allp[sel], allc[sel]
         rp, col, _ = el.csr()
         kid = np.full(el.n, -1, np.int64)
@@ -357,6 +359,8 @@ def run_extra(args):
     import fastbc_gpu as fg
 
     fg.init(0)
+    if args.ws_budget_mb > 0:
+        fg.set_option("ws_budget_mb", args.ws_budget_mb)
     prec = fg.FP32C if args.prec == "fp32c" else fg.FP64
     sched = fg.BATCHED if args.sched == "batched" else fg.PLAIN
     wl = EXTRA_WORKLOADS[args.workload]()
@@ -394,7 +398,7 @@ def run_extra(args):
     if len(phases) > 1:
         line["phases"] = [{"device_ms_per_step": ms / args.steps, "gteps": rel / ms / 1e6 if ms else None}
                           for ms, rel in (phases[i] for i in sorted(phases))]
-    if args.workload == "grid2048-clustered" and args.prec == "fp32c":
+    if args.workload == "grid2048-clustered" and args.prec == "fp32c" and not args.no_precision:
         wl.step(fg, fg.FP64, sched)
         ref = wl.last.copy()
         wl.step(fg, fg.FP32C, sched)
@@ -406,7 +410,7 @@ def run_extra(args):
             "mean_rel_large": float(np.mean(np.abs(got[big] - ref[big]) / np.abs(ref[big]))),
             "reference": "the FP64 form on the GPU; the clustered BC is a cancellation, so entries "
                          "below 1e-3 of the largest are bounded through max_abs_over_max"}
-    if args.workload in ("grid512-exact", "grid32-exact") and args.prec == "fp32c":
+    if args.workload in ("grid512-exact", "grid32-exact") and args.prec == "fp32c" and not args.no_precision:
         wl.step(fg, fg.FP64, sched)
         ref = wl.last.copy()
         wl.step(fg, fg.FP32C, sched)
@@ -474,6 +478,12 @@ def main():
                     help="batched schedule: keep the default knobs instead of tuning them first")
     ap.add_argument("--small", action="store_true",
                     help="profiling case: 8 clusters and 256 pivots of the same workload")
+    ap.add_argument("--max-pivots", type=int, default=0,
+                    help="grid2048-clustered: at most this many pivots per step (profiling cases)")
+    ap.add_argument("--no-precision", action="store_true",
+                    help="extra workloads: skip the FP32C-vs-FP64 comparison runs")
+    ap.add_argument("--ws-budget-mb", type=int, default=0,
+                    help="cap the block kernels' workspace (fewer concurrent sources; profiling cases)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -492,6 +502,8 @@ def main():
     import fastbc_gpu as fg
 
     fg.init(local)
+    if args.ws_budget_mb > 0:
+        fg.set_option("ws_budget_mb", args.ws_budget_mb)
     prec = fg.FP32C if args.prec == "fp32c" else fg.FP64
     sched = fg.BATCHED if args.sched == "batched" else fg.PLAIN
     el, z = load_workload()

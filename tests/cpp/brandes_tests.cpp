@@ -72,7 +72,7 @@ int main(int argc, char** argv) {
             o.sched = sched;
             // "Exact Brandes' BC computation test" (ExactBrandesBC.cpp:11-35), on the subgraph
             auto bc = fbcgpu::exact_bc<float>(sub, o);
-            REQUIRE(bc.size() == 9);
+            REQUIRE(bc.size() == sub.vertices().size());  // sized as ExactBrandesBC.h:49 sizes it
             REQUIRE(bc[0] == 2.0f);
             REQUIRE(bc[1] == 2.0f);
             REQUIRE(bc[2] == 0.5f);
