@@ -443,13 +443,15 @@ int launch_block(const Plan& P, const std::vector<Unit>& units_in, int ws_n, fbc
     std::vector<Unit> units;
     const int64_t budget = ws_budget();
     if (fr) {
-        // sources per block: one unless option "group" asks for 2 or 4 (sharing rounds and
-        // levels pays only where a source's frontier is much narrower than the block; on
-        // road-like graphs one source per block measured faster at every size tried)
+        // sources per block (option "group" forces one): sharing rounds and levels pays where
+        // a source's frontier is much narrower than the block -- segments of up to 32K
+        // vertices (Louvain clusters: 4 per block measured 1.26x one per block); whole
+        // graphs of 64K+ vertices measured faster one per block.  K > 1 also needs a group
+        // for every block slot.
         const int forced = (int)g.opt.group;
         const int cand[3] = {4, 2, 1};
         for (int K : cand) {
-            if (K != (forced > 0 ? forced : 1)) continue;
+            if (forced > 0 ? K != forced : (K > 1 && ws_n > 32768)) continue;
             if ((int64_t)ws_n * K >= ((int64_t)1 << 31) - 1) continue;
             KernFn f = frontier_variant<Prec>(wide, K);
             int b = 0;
