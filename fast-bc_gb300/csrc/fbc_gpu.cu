@@ -14,6 +14,7 @@
 #include <string>
 #include <vector>
 
+#include "cluster_build.cuh"
 #include "frontier_kernels.cuh"
 
 namespace {
@@ -111,6 +112,8 @@ struct Ctx {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, evm = nullptr;
     Options opt;
     DBuf retry, segs, units_b, units_w, chunks, crp, cadj, cgid, cbord, bc, bdist, bsig, ctr, dbg;
+    // cluster extraction scratch: offsets, ids, flags, scans, given borders, error word
+    DBuf c_off, c_id, c_lid, c_isb, c_flag, c_scan, c_sums, c_boff, c_bsrc, c_m, c_err;
     Workspace wsb, wsw;
 };
 Ctx g;
@@ -743,125 +746,215 @@ int download_bc(double* out, int64_t len, bool accumulate, fbc_stats* st) {
 
 // Border vertices of each cluster: a member with an in- or out-edge crossing the cluster
 // (SubGraph.h:70-135), ascending global id (the std::set order of SubGraph::borders).
-void compute_borders(const fbc_graph_s* G, int32_t nclusters, const int64_t* coff,
-                     const int32_t* cverts, const std::vector<int32_t>& cid,
-                     std::vector<int64_t>& boff, std::vector<int32_t>& bl) {
-    std::vector<char> isb((size_t)G->n, 0);
-    for (int32_t v = 0; v < G->n; ++v)
-        for (int64_t e = G->h_rp[v]; e < G->h_rp[v + 1]; ++e) {
-            const int32_t x = G->h_col[e];
-            if (cid[v] != cid[x]) {
-                isb[v] = 1;
-                isb[x] = 1;
-            }
-        }
-    boff.assign((size_t)nclusters + 1, 0);
-    bl.clear();
-    for (int32_t c = 0; c < nclusters; ++c) {
-        std::vector<int32_t> b;
-        for (int64_t i = coff[c]; i < coff[c + 1]; ++i)
-            if (isb[cverts[i]]) b.push_back(cverts[i]);
-        std::sort(b.begin(), b.end());
-        bl.insert(bl.end(), b.begin(), b.end());
-        boff[c + 1] = (int64_t)bl.size();
-    }
+// kernels launched by the cluster-build helpers since the counter was last read
+int g_aux_launches = 0;
+
+unsigned grid_for(int64_t items, int threads = 256) {
+    ++g_aux_launches;  // every caller launches one kernel with the returned grid
+    return (unsigned)std::max<int64_t>(1, std::min<int64_t>((items + threads - 1) / threads, (int64_t)g.nsm * 16));
 }
 
-int cluster_ids(const fbc_graph_s* G, int32_t nclusters, const int64_t* coff, const int32_t* cverts,
-                std::vector<int32_t>& cid) {
+// Exclusive scan of `len` int32 values on the library stream: out[0 .. len] (len + 1 entries).
+int device_scan(const int32_t* in, int64_t len, int32_t* out) {
+    if (len <= 0) {
+        FBC_CK(cudaMemsetAsync(out, 0, sizeof(int32_t), g.st));
+        return FBC_OK;
+    }
+    const int64_t nb = (len + fbc::kScanBlock - 1) / fbc::kScanBlock;
+    g_aux_launches += 3;
+    FBC_CK(g.c_sums.ensure(sizeof(int32_t) * (size_t)nb));
+    int32_t* sums = g.c_sums.as<int32_t>();
+    fbc::scan_sums_kernel<<<(unsigned)nb, fbc::kScanBlock, 0, g.st>>>(in, len, sums);
+    fbc::scan_top_kernel<<<1, fbc::kScanBlock, 0, g.st>>>(sums, nb);
+    fbc::scan_apply_kernel<<<(unsigned)nb, fbc::kScanBlock, 0, g.st>>>(in, len, sums, out);
+    FBC_CK(cudaGetLastError());
+    return FBC_OK;
+}
+
+int check_cluster_offsets(const fbc_graph_s* G, int32_t nclusters, const int64_t* coff, const int32_t* cverts) {
     if (nclusters < 0 || !coff || (nclusters > 0 && !cverts))
         return fail(FBC_ERR_INVALID_ARG, "bad cluster arrays");
-    cid.assign((size_t)G->n, -1);
     if (coff[0] != 0) return fail(FBC_ERR_INVALID_ARG, "cluster_off[0] must be 0");
-    for (int32_t c = 0; c < nclusters; ++c) {
+    for (int32_t c = 0; c < nclusters; ++c)
         if (coff[c + 1] < coff[c]) return fail(FBC_ERR_INVALID_ARG, "cluster_off is not monotone");
-        for (int64_t i = coff[c]; i < coff[c + 1]; ++i) {
-            const int32_t v = cverts[i];
-            if (v < 0 || v >= G->n) return fail(FBC_ERR_INVALID_ARG, "cluster vertex id out of range");
-            if (cid[v] != -1) return fail(FBC_ERR_INVALID_ARG, "vertex listed in two clusters or twice");
-            cid[v] = c;
-        }
+    if (coff[nclusters] > (int64_t)G->n) return fail(FBC_ERR_INVALID_ARG, "vertex listed in two clusters or twice");
+    return FBC_OK;
+}
+
+int cluster_error(int e) {
+    if (e & fbc::kCluRange) return fail(FBC_ERR_INVALID_ARG, "cluster vertex id out of range");
+    if (e & fbc::kCluDup) return fail(FBC_ERR_INVALID_ARG, "vertex listed in two clusters or twice");
+    if (e & fbc::kCluBorder) return fail(FBC_ERR_INVALID_ARG, "border vertex not in its cluster");
+    return FBC_OK;
+}
+
+// Cluster ids on the device (g.c_id, g.c_lid; g.cgid holds the cluster vertex lists), the
+// offsets in g.c_off; the error word is cleared.
+int device_cluster_ids(const fbc_graph_s* G, int32_t nclusters, const int64_t* coff, const int32_t* cverts,
+                       fbc_stats* st) {
+    FBC_TRY(check_cluster_offsets(G, nclusters, coff, cverts));
+    const int64_t nv = coff[nclusters];
+    const int32_t n = G->n;
+    FBC_CK(g.c_off.ensure(sizeof(int64_t) * ((size_t)nclusters + 1)));
+    FBC_CK(g.cgid.ensure(sizeof(int32_t) * (size_t)std::max<int64_t>(nv, 1)));
+    FBC_CK(g.c_id.ensure(sizeof(int32_t) * (size_t)std::max(n, 1)));
+    FBC_CK(g.c_lid.ensure(sizeof(int32_t) * (size_t)std::max(n, 1)));
+    FBC_CK(g.c_err.ensure(64));
+    FBC_CK(cudaMemcpyAsync(g.c_off.p, coff, sizeof(int64_t) * ((size_t)nclusters + 1), cudaMemcpyHostToDevice, g.st));
+    if (nv > 0)
+        FBC_CK(cudaMemcpyAsync(g.cgid.p, cverts, sizeof(int32_t) * (size_t)nv, cudaMemcpyHostToDevice, g.st));
+    FBC_CK(cudaMemsetAsync(g.c_id.p, 0xff, sizeof(int32_t) * (size_t)std::max(n, 1), g.st));
+    FBC_CK(cudaMemsetAsync(g.c_err.p, 0, 64, g.st));
+    if (st) st->h2d_bytes += (int64_t)(sizeof(int64_t) * ((size_t)nclusters + 1) + sizeof(int32_t) * (size_t)nv);
+    if (nv > 0) {
+        fbc::clu_ids_kernel<<<grid_for(nv), 256, 0, g.st>>>(nv, g.c_off.as<int64_t>(), nclusters, g.cgid.as<int32_t>(),
+                                                            n, g.c_id.as<int32_t>(), g.c_lid.as<int32_t>(),
+                                                            g.c_err.as<int>());
+        FBC_CK(cudaGetLastError());
+        // every later kernel indexes rows by these ids: stop here on a bad list
+        int err = 0;
+        FBC_CK(cudaMemcpyAsync(&err, g.c_err.p, sizeof(int), cudaMemcpyDeviceToHost, g.st));
+        FBC_CK(cudaStreamSynchronize(g.st));
+        FBC_TRY(cluster_error(err));
     }
     return FBC_OK;
 }
 
-// Host side of a batched cluster evaluation: cluster ids, borders (computed when not given),
-// the induced-subgraph CSR of every cluster with local ids (SubGraph::forwardStar keeps the
-// intra-cluster edges), uploaded into the given device buffers, and the plan's segments and
-// units (border-output row of the i-th vertex of cluster c: E_c + i * nb_c).
+// Border discovery on the device (after device_cluster_ids): boff (nclusters + 1) and the
+// borders of every cluster in ascending id, on the host; the device copy (global ids) stays in
+// g.c_bsrc with the offsets in g.c_boff.
+int device_borders(const fbc_graph_s* G, int32_t nclusters, const int64_t* coff, std::vector<int64_t>& boff,
+                   std::vector<int32_t>& bl, fbc_stats* st) {
+    const int64_t nv = coff[nclusters];
+    const int32_t n = G->n;
+    FBC_CK(g.c_isb.ensure((size_t)std::max(n, 1)));
+    FBC_CK(g.c_flag.ensure(sizeof(int32_t) * (size_t)std::max<int64_t>(nv, 1)));
+    FBC_CK(g.c_scan.ensure(sizeof(int32_t) * (size_t)(nv + 1)));
+    FBC_CK(cudaMemsetAsync(g.c_isb.p, 0, (size_t)std::max(n, 1), g.st));
+    if (n > 0)
+        fbc::clu_border_flag_kernel<<<grid_for(n), 256, 0, g.st>>>(n, G->d_rp, G->d_adj, g.c_id.as<int32_t>(),
+                                                                   g.c_isb.as<uint8_t>());
+    if (nv > 0)
+        fbc::clu_gather_flag_kernel<<<grid_for(nv), 256, 0, g.st>>>(nv, g.cgid.as<int32_t>(), g.c_isb.as<uint8_t>(),
+                                                                    g.c_flag.as<int32_t>());
+    FBC_CK(cudaGetLastError());
+    FBC_TRY(device_scan(g.c_flag.as<int32_t>(), nv, g.c_scan.as<int32_t>()));
+    // border offsets: the scan at every cluster start
+    std::vector<int32_t> pos((size_t)nv + 1);
+    FBC_CK(cudaMemcpyAsync(pos.data(), g.c_scan.p, sizeof(int32_t) * pos.size(), cudaMemcpyDeviceToHost, g.st));
+    FBC_CK(cudaStreamSynchronize(g.st));
+    boff.assign((size_t)nclusters + 1, 0);
+    for (int32_t c = 0; c <= nclusters; ++c) boff[c] = pos[coff[c]];
+    const int64_t nb = boff[nclusters];
+    FBC_CK(g.c_bsrc.ensure(sizeof(int32_t) * (size_t)std::max<int64_t>(nb, 1)));
+    FBC_CK(g.c_boff.ensure(sizeof(int64_t) * ((size_t)nclusters + 1)));
+    if (nv > 0)
+        fbc::clu_border_scatter_kernel<<<grid_for(nv), 256, 0, g.st>>>(
+            nv, g.c_off.as<int64_t>(), nclusters, g.cgid.as<int32_t>(), g.c_flag.as<int32_t>(),
+            g.c_scan.as<int32_t>(), g.c_bsrc.as<int32_t>(), g.c_err.as<int>());
+    FBC_CK(cudaGetLastError());
+    bl.resize((size_t)nb);
+    int err = 0;
+    if (nb > 0)
+        FBC_CK(cudaMemcpyAsync(bl.data(), g.c_bsrc.p, sizeof(int32_t) * (size_t)nb, cudaMemcpyDeviceToHost, g.st));
+    FBC_CK(cudaMemcpyAsync(&err, g.c_err.p, sizeof(int), cudaMemcpyDeviceToHost, g.st));
+    FBC_CK(cudaStreamSynchronize(g.st));
+    if (st) st->d2h_bytes += (int64_t)(sizeof(int32_t) * ((size_t)nv + 1 + (size_t)nb));
+    FBC_TRY(cluster_error(err));
+    if (err & fbc::kCluOrder) {  // cluster lists not ascending: sort every cluster's borders
+        for (int32_t c = 0; c < nclusters; ++c) std::sort(bl.begin() + boff[c], bl.begin() + boff[c + 1]);
+        if (nb > 0)
+            FBC_CK(cudaMemcpyAsync(g.c_bsrc.p, bl.data(), sizeof(int32_t) * (size_t)nb, cudaMemcpyHostToDevice, g.st));
+    }
+    FBC_CK(cudaMemcpyAsync(g.c_boff.p, boff.data(), sizeof(int64_t) * boff.size(), cudaMemcpyHostToDevice, g.st));
+    FBC_CK(cudaStreamSynchronize(g.st));
+    return FBC_OK;
+}
+
+// A batched cluster evaluation's device side: cluster ids, borders (discovered when not
+// given), the induced-subgraph CSR of every cluster with local ids (SubGraph::forwardStar keeps
+// the intra-cluster edges) built by device kernels into the given buffers, and the plan's
+// segments and units (border-output row of the i-th vertex of cluster c: E_c + i * nb_c).
 int prepare_clusters(const fbc_graph_s* G, int32_t nclusters, const int64_t* coff, const int32_t* cverts,
                      const int64_t* border_off, const int32_t* borders, int precision, int sched,
                      DBuf& crp, DBuf& cadj, DBuf& cgid, DBuf& cbord, Plan& P, int64_t& ent, fbc_stats* st) {
-    std::vector<int32_t> cid;
-    FBC_TRY(cluster_ids(G, nclusters, coff, cverts, cid));
+    g_aux_launches = 0;
+    FBC_TRY(device_cluster_ids(G, nclusters, coff, cverts, st));
+    const int64_t nv = coff[nclusters];
     std::vector<int64_t> boff_v;
     std::vector<int32_t> bl_v;
     if (!border_off) {
-        compute_borders(G, nclusters, coff, cverts, cid, boff_v, bl_v);
+        FBC_TRY(device_borders(G, nclusters, coff, boff_v, bl_v, st));
         border_off = boff_v.data();
-        borders = bl_v.data();
+    } else {
+        if (border_off[0] != 0) return fail(FBC_ERR_INVALID_ARG, "border_off[0] must be 0");
+        for (int32_t c = 0; c < nclusters; ++c)
+            if (border_off[c + 1] < border_off[c]) return fail(FBC_ERR_INVALID_ARG, "border_off is not monotone");
+        const int64_t nb = border_off[nclusters];
+        FBC_CK(g.c_bsrc.ensure(sizeof(int32_t) * (size_t)std::max<int64_t>(nb, 1)));
+        FBC_CK(g.c_boff.ensure(sizeof(int64_t) * ((size_t)nclusters + 1)));
+        if (nb > 0)
+            FBC_CK(cudaMemcpyAsync(g.c_bsrc.p, borders, sizeof(int32_t) * (size_t)nb, cudaMemcpyHostToDevice, g.st));
+        FBC_CK(cudaMemcpyAsync(g.c_boff.p, border_off, sizeof(int64_t) * ((size_t)nclusters + 1),
+                               cudaMemcpyHostToDevice, g.st));
+        if (st) st->h2d_bytes += (int64_t)(sizeof(int32_t) * (size_t)nb + sizeof(int64_t) * ((size_t)nclusters + 1));
     }
-    std::vector<int32_t> lid((size_t)G->n, -1);
-    for (int32_t c = 0; c < nclusters; ++c)
-        for (int64_t i = coff[c]; i < coff[c + 1]; ++i) lid[cverts[i]] = (int32_t)(i - coff[c]);
-    const int64_t nv = coff[nclusters];
-    std::vector<int32_t> hrp;
-    std::vector<int2> hadj;
-    std::vector<int32_t> hbord;
-    std::vector<int64_t> rp_off((size_t)nclusters), adj_off((size_t)nclusters), b_off((size_t)nclusters);
-    std::vector<int64_t> seg_m((size_t)nclusters);
-    hrp.reserve((size_t)(nv + nclusters));
-    for (int32_t c = 0; c < nclusters; ++c) {
-        rp_off[c] = (int64_t)hrp.size();
-        adj_off[c] = (int64_t)hadj.size();
-        int32_t e = 0;
-        hrp.push_back(0);
-        for (int64_t i = coff[c]; i < coff[c + 1]; ++i) {
-            const int32_t v = cverts[i];
-            for (int64_t k = G->h_rp[v]; k < G->h_rp[v + 1]; ++k) {
-                const int32_t x = G->h_col[k];
-                if (cid[x] == c) {
-                    hadj.push_back(make_int2(lid[x], G->h_w[k]));
-                    ++e;
-                }
-            }
-            hrp.push_back(e);
-        }
-        seg_m[c] = e;
-        b_off[c] = (int64_t)hbord.size();
-        for (int64_t j = border_off[c]; j < border_off[c + 1]; ++j) {
-            const int32_t b = borders[j];
-            if (b < 0 || b >= G->n || cid[b] != c)
-                return fail(FBC_ERR_INVALID_ARG, "border vertex not in its cluster");
-            hbord.push_back(lid[b]);
-        }
-    }
-    FBC_CK(crp.ensure(sizeof(int32_t) * std::max<size_t>(hrp.size(), 1)));
-    FBC_CK(cadj.ensure(sizeof(int2) * std::max<size_t>(hadj.size(), 1)));
-    FBC_CK(cgid.ensure(sizeof(int32_t) * std::max<int64_t>(nv, 1)));
-    FBC_CK(cbord.ensure(sizeof(int32_t) * std::max<size_t>(hbord.size(), 1)));
-    if (!hrp.empty())
-        FBC_CK(cudaMemcpyAsync(crp.p, hrp.data(), sizeof(int32_t) * hrp.size(), cudaMemcpyHostToDevice, g.st));
-    if (!hadj.empty())
-        FBC_CK(cudaMemcpyAsync(cadj.p, hadj.data(), sizeof(int2) * hadj.size(), cudaMemcpyHostToDevice, g.st));
+    const int64_t nbt = border_off[nclusters];
+    // intra-cluster degrees, their scan, the local CSRs and the local border ids
+    FBC_CK(g.c_flag.ensure(sizeof(int32_t) * (size_t)std::max<int64_t>(nv, 1)));
+    FBC_CK(g.c_scan.ensure(sizeof(int32_t) * (size_t)(nv + 1)));
+    FBC_CK(g.c_m.ensure(sizeof(int64_t) * 2 * (size_t)std::max(nclusters, 1)));
+    FBC_CK(crp.ensure(sizeof(int32_t) * (size_t)std::max<int64_t>(nv + nclusters, 1)));
+    FBC_CK(cbord.ensure(sizeof(int32_t) * (size_t)std::max<int64_t>(nbt, 1)));
     if (nv > 0)
-        FBC_CK(cudaMemcpyAsync(cgid.p, cverts, sizeof(int32_t) * (size_t)nv, cudaMemcpyHostToDevice, g.st));
-    if (!hbord.empty())
-        FBC_CK(cudaMemcpyAsync(cbord.p, hbord.data(), sizeof(int32_t) * hbord.size(), cudaMemcpyHostToDevice, g.st));
-    FBC_CK(cudaStreamSynchronize(g.st));  // the host vectors go out of scope
-    if (st)
-        st->h2d_bytes += (int64_t)(sizeof(int32_t) * (hrp.size() + (size_t)nv + hbord.size()) +
-                                   sizeof(int2) * hadj.size());
+        fbc::clu_degree_kernel<<<grid_for(nv), 256, 0, g.st>>>(nv, g.cgid.as<int32_t>(), G->d_rp, G->d_adj,
+                                                               g.c_id.as<int32_t>(), g.c_flag.as<int32_t>());
+    FBC_CK(cudaGetLastError());
+    FBC_TRY(device_scan(g.c_flag.as<int32_t>(), nv, g.c_scan.as<int32_t>()));
+    int32_t medges = 0;
+    FBC_CK(cudaMemcpyAsync(&medges, g.c_scan.as<int32_t>() + nv, sizeof(int32_t), cudaMemcpyDeviceToHost, g.st));
+    FBC_CK(cudaStreamSynchronize(g.st));
+    FBC_CK(cadj.ensure(sizeof(int2) * (size_t)std::max(medges, 1)));
+    if (nv > 0)
+        fbc::clu_fill_kernel<<<grid_for(nv), 256, 0, g.st>>>(nv, g.c_off.as<int64_t>(), nclusters, g.cgid.as<int32_t>(),
+                                                             G->d_rp, G->d_adj, g.c_id.as<int32_t>(),
+                                                             g.c_lid.as<int32_t>(), g.c_scan.as<int32_t>(),
+                                                             crp.as<int32_t>(), cadj.as<int2>());
+    if (nclusters > 0)
+        fbc::clu_close_kernel<<<grid_for(nclusters), 256, 0, g.st>>>(nclusters, g.c_off.as<int64_t>(),
+                                                                     g.c_scan.as<int32_t>(), crp.as<int32_t>(),
+                                                                     g.c_m.as<int64_t>(),
+                                                                     g.c_m.as<int64_t>() + nclusters);
+    if (nbt > 0)
+        fbc::clu_border_map_kernel<<<grid_for(nbt), 256, 0, g.st>>>(nbt, g.c_boff.as<int64_t>(), nclusters,
+                                                                    g.c_bsrc.as<int32_t>(), G->n, g.c_id.as<int32_t>(),
+                                                                    g.c_lid.as<int32_t>(), cbord.as<int32_t>(),
+                                                                    g.c_err.as<int>());
+    FBC_CK(cudaGetLastError());
+    // per cluster: edge count and first edge (the scan at the cluster's first vertex)
+    std::vector<int64_t> seg_m(2 * (size_t)std::max(nclusters, 1), 0);
+    int err = 0;
+    if (nclusters > 0)
+        FBC_CK(cudaMemcpyAsync(seg_m.data(), g.c_m.p, sizeof(int64_t) * 2 * (size_t)nclusters, cudaMemcpyDeviceToHost, g.st));
+    FBC_CK(cudaMemcpyAsync(&err, g.c_err.p, sizeof(int), cudaMemcpyDeviceToHost, g.st));
+    FBC_CK(cudaStreamSynchronize(g.st));
+    FBC_TRY(cluster_error(err));
+    // the cluster vertex lists are the output index maps of the segments
+    if (&cgid != &g.cgid && nv > 0) {
+        FBC_CK(cgid.ensure(sizeof(int32_t) * (size_t)nv));
+        FBC_CK(cudaMemcpyAsync(cgid.p, g.cgid.p, sizeof(int32_t) * (size_t)nv, cudaMemcpyDeviceToDevice, g.st));
+        FBC_CK(cudaStreamSynchronize(g.st));
+    }
     P.prec = precision;
     P.sched = sched;
     ent = 0;
     const int dl = delta_for(G->meanw);
     for (int32_t c = 0; c < nclusters; ++c) {
         Seg s{};
-        s.rp = crp.as<int32_t>() + rp_off[c];
-        s.adj = cadj.as<int2>() + adj_off[c];
+        s.rp = crp.as<int32_t>() + coff[c] + c;
+        s.adj = cadj.as<int2>() + seg_m[(size_t)nclusters + c];  // rows are relative to the first edge
         s.gid = cgid.as<int32_t>() + coff[c];
-        s.border = cbord.as<int32_t>() + b_off[c];
+        s.border = cbord.as<int32_t>() + border_off[c];
         s.out_base = 0;
         s.n = (int32_t)(coff[c + 1] - coff[c]);
         s.nb = (int32_t)(border_off[c + 1] - border_off[c]);
@@ -875,6 +968,7 @@ int prepare_clusters(const fbc_graph_s* G, int32_t nclusters, const int64_t* cof
     }
     P.bc_len = G->n;
     P.border_entries = ent;
+    if (st) st->launches += g_aux_launches;
     return FBC_OK;
 }
 
@@ -913,7 +1007,8 @@ int fbc_gpu_shutdown(void) {
     std::lock_guard<std::recursive_mutex> lk(g_mu);
     if (!g.init) return FBC_OK;
     cudaStreamSynchronize(g.st);
-    for (DBuf* b : {&g.retry, &g.segs, &g.units_b, &g.units_w, &g.chunks, &g.crp, &g.cadj, &g.cgid, &g.cbord, &g.bc,
+    for (DBuf* b : {&g.c_off, &g.c_id, &g.c_lid, &g.c_isb, &g.c_flag, &g.c_scan, &g.c_sums, &g.c_boff,
+                    &g.c_bsrc, &g.c_m, &g.c_err, &g.retry, &g.segs, &g.units_b, &g.units_w, &g.chunks, &g.crp, &g.cadj, &g.cgid, &g.cbord, &g.bc,
                     &g.bdist, &g.bsig, &g.ctr, &g.dbg})
         b->release();
     g.wsb.buf.release();
@@ -1143,14 +1238,16 @@ int fbc_cluster_border_count(fbc_graph G, int32_t nclusters, const int64_t* coff
                              const int32_t* cverts, const int64_t* border_off, int64_t* out_nb,
                              int64_t* out_entries) {
     std::lock_guard<std::recursive_mutex> lk(g_mu);
+    FBC_TRY(check_init());
     if (!G) return fail(FBC_ERR_INVALID_ARG, "null graph");
-    std::vector<int32_t> cid;
-    FBC_TRY(cluster_ids(G, nclusters, coff, cverts, cid));
     std::vector<int64_t> boff;
     std::vector<int32_t> bl;
     if (!border_off) {
-        compute_borders(G, nclusters, coff, cverts, cid, boff, bl);
+        FBC_TRY(device_cluster_ids(G, nclusters, coff, cverts, nullptr));
+        FBC_TRY(device_borders(G, nclusters, coff, boff, bl, nullptr));
         border_off = boff.data();
+    } else {
+        FBC_TRY(check_cluster_offsets(G, nclusters, coff, cverts));
     }
     int64_t nb = 0, ent = 0;
     for (int32_t c = 0; c < nclusters; ++c) {
@@ -1166,12 +1263,12 @@ int fbc_cluster_border_count(fbc_graph G, int32_t nclusters, const int64_t* coff
 int fbc_cluster_borders(fbc_graph G, int32_t nclusters, const int64_t* coff, const int32_t* cverts,
                         int64_t* out_boff, int32_t* out_borders) {
     std::lock_guard<std::recursive_mutex> lk(g_mu);
+    FBC_TRY(check_init());
     if (!G) return fail(FBC_ERR_INVALID_ARG, "null graph");
-    std::vector<int32_t> cid;
-    FBC_TRY(cluster_ids(G, nclusters, coff, cverts, cid));
     std::vector<int64_t> boff;
     std::vector<int32_t> bl;
-    compute_borders(G, nclusters, coff, cverts, cid, boff, bl);
+    FBC_TRY(device_cluster_ids(G, nclusters, coff, cverts, nullptr));
+    FBC_TRY(device_borders(G, nclusters, coff, boff, bl, nullptr));
     if (out_boff) std::copy(boff.begin(), boff.end(), out_boff);
     if (out_borders) std::copy(bl.begin(), bl.end(), out_borders);
     return FBC_OK;
