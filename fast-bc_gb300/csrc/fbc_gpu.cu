@@ -15,6 +15,7 @@
 #include <vector>
 
 #include "cluster_build.cuh"
+#include "graph_build.cuh"
 #include "frontier_kernels.cuh"
 
 namespace {
@@ -89,6 +90,7 @@ struct Options {
     int64_t ws_budget_mb = 0;   // 0 = 60% of the free device memory
     int64_t group = 0;          // frontier kernel sources per block (1, 2, 4); 0 = automatic
     int64_t order_min_n = 131072;  // batched runs relabel graphs of at least this many vertices
+    int64_t csr_device_min_m = 65536;  // edge lists of at least this many edges are built on the device
     int64_t warp_smem = 1;      // batched: warp state in shared memory when it fits
     int64_t debug_sched = FBC_SCHED_PLAIN;  // schedule used by fbc_sssp_debug
 };
@@ -972,6 +974,124 @@ int prepare_clusters(const fbc_graph_s* G, int32_t nclusters, const int64_t* cof
     return FBC_OK;
 }
 
+// A device buffer released when it goes out of scope (temporaries of a graph build).
+struct TmpBuf : DBuf {
+    TmpBuf() = default;
+    TmpBuf(const TmpBuf&) = delete;
+    ~TmpBuf() { release(); }
+};
+
+// Edge list -> device CSR (graph_build.cuh).  Returns FBC_OK with *out set, FBC_OK with *out
+// null when a row is longer than the device sort handles (the caller then builds on the host),
+// or an error.
+int device_graph_from_edges(int64_t count, const int32_t* src, const int32_t* dst, const double* w,
+                            fbc_graph* out) {
+    *out = nullptr;
+    TmpBuf dsrc, ddst, dw, ints, deg, rs, cursor, keys, ndeg, indeg;
+    FBC_CK(dsrc.ensure(sizeof(int32_t) * (size_t)count));
+    FBC_CK(ddst.ensure(sizeof(int32_t) * (size_t)count));
+    FBC_CK(dw.ensure(sizeof(double) * (size_t)count));
+    FBC_CK(ints.ensure(64));
+    FBC_CK(cudaMemcpyAsync(dsrc.p, src, sizeof(int32_t) * (size_t)count, cudaMemcpyHostToDevice, g.st));
+    FBC_CK(cudaMemcpyAsync(ddst.p, dst, sizeof(int32_t) * (size_t)count, cudaMemcpyHostToDevice, g.st));
+    FBC_CK(cudaMemcpyAsync(dw.p, w, sizeof(double) * (size_t)count, cudaMemcpyHostToDevice, g.st));
+    // ints: [0] max source, [1] error bits, [2] max weight, [3] max in-degree, [4..5] weight sum
+    int hi[6] = {-1, 0, 0, 0, 0, 0};
+    FBC_CK(cudaMemcpyAsync(ints.p, hi, sizeof(hi), cudaMemcpyHostToDevice, g.st));
+    int* di = ints.as<int>();
+    fbc::gb_check_kernel<<<grid_for(count), 256, 0, g.st>>>(count, dsrc.as<int32_t>(), ddst.as<int32_t>(),
+                                                            dw.as<double>(), di, di + 1);
+    FBC_CK(cudaGetLastError());
+    FBC_CK(cudaMemcpyAsync(hi, ints.p, 2 * sizeof(int), cudaMemcpyDeviceToHost, g.st));
+    FBC_CK(cudaStreamSynchronize(g.st));
+    if (hi[1] & fbc::kGbWeight) return fail(FBC_ERR_INVALID_ARG, "Edge weight must be greater than zero");
+    if (hi[1] & fbc::kGbNegId) return fail(FBC_ERR_INVALID_ARG, "negative vertex id");
+    const int32_t n = hi[0] + 1;
+    FBC_CK(deg.ensure(sizeof(int32_t) * (size_t)n));
+    FBC_CK(rs.ensure(sizeof(int32_t) * ((size_t)n + 1)));
+    FBC_CK(cursor.ensure(sizeof(int32_t) * (size_t)n));
+    FBC_CK(keys.ensure(sizeof(unsigned long long) * (size_t)count));
+    FBC_CK(ndeg.ensure(sizeof(int32_t) * (size_t)n));
+    FBC_CK(cudaMemsetAsync(deg.p, 0, sizeof(int32_t) * (size_t)n, g.st));
+    FBC_CK(cudaMemsetAsync(cursor.p, 0, sizeof(int32_t) * (size_t)n, g.st));
+    fbc::gb_count_kernel<<<grid_for(count), 256, 0, g.st>>>(count, dsrc.as<int32_t>(), ddst.as<int32_t>(), n,
+                                                            deg.as<int32_t>(), di + 1);
+    FBC_CK(cudaGetLastError());
+    FBC_TRY(device_scan(deg.as<int32_t>(), n, rs.as<int32_t>()));
+    fbc::gb_scatter_kernel<<<grid_for(count), 256, 0, g.st>>>(count, dsrc.as<int32_t>(), ddst.as<int32_t>(),
+                                                              rs.as<int32_t>(), cursor.as<int32_t>(),
+                                                              keys.as<unsigned long long>());
+    fbc::gb_sort_rows_kernel<<<grid_for(n), 256, 0, g.st>>>(n, rs.as<int32_t>(), keys.as<unsigned long long>(),
+                                                            ndeg.as<int32_t>(), di + 1);
+    FBC_CK(cudaGetLastError());
+    FBC_CK(cudaMemcpyAsync(hi + 1, di + 1, sizeof(int), cudaMemcpyDeviceToHost, g.st));
+    FBC_CK(cudaStreamSynchronize(g.st));
+    if (hi[1] & fbc::kGbDst) return fail(FBC_ERR_INVALID_ARG, "destination id is not below 1 + max source id");
+    if (hi[1] & fbc::kGbLongRow) return FBC_OK;  // host path
+    auto* G = new fbc_graph_s();
+    std::unique_ptr<fbc_graph_s> guard(G);
+    G->n = n;
+    const cudaError_t ea = cudaMalloc(&G->d_rp, sizeof(int32_t) * ((size_t)n + 1));
+    if (ea != cudaSuccess) {
+        G->d_rp = nullptr;
+        return fail(FBC_ERR_OOM, "device allocation of the graph failed");
+    }
+    auto drop = [&]() {
+        if (G->d_rp) cudaFree(G->d_rp);
+        if (G->d_adj) cudaFree(G->d_adj);
+        G->d_rp = nullptr;
+        G->d_adj = nullptr;
+    };
+    if (device_scan(ndeg.as<int32_t>(), n, G->d_rp) != FBC_OK) { drop(); return FBC_ERR_CUDA; }
+    int32_t medges = 0;
+    if (cudaMemcpyAsync(&medges, G->d_rp + n, sizeof(int32_t), cudaMemcpyDeviceToHost, g.st) != cudaSuccess ||
+        cudaStreamSynchronize(g.st) != cudaSuccess) { drop(); return fail(FBC_ERR_CUDA, "graph build failed"); }
+    if (cudaMalloc(&G->d_adj, sizeof(int2) * (size_t)std::max(medges, 1)) != cudaSuccess) {
+        G->d_adj = nullptr;
+        drop();
+        return fail(FBC_ERR_OOM, "device allocation of the graph failed");
+    }
+    if (indeg.ensure(sizeof(int32_t) * (size_t)n) != cudaSuccess ||
+        cudaMemsetAsync(indeg.p, 0, sizeof(int32_t) * (size_t)n, g.st) != cudaSuccess) {
+        drop();
+        return fail(FBC_ERR_OOM, "device allocation failed");
+    }
+    fbc::gb_merge_kernel<<<grid_for(n), 256, 0, g.st>>>(n, rs.as<int32_t>(), keys.as<unsigned long long>(),
+                                                        dw.as<double>(), G->d_rp, G->d_adj, indeg.as<int32_t>(),
+                                                        di + 2, (unsigned long long*)(di + 4), di + 1);
+    fbc::gb_max_kernel<<<grid_for(n), 256, 0, g.st>>>(n, indeg.as<int32_t>(), di + 3);
+    std::vector<int32_t> rp32((size_t)n + 1);
+    std::vector<int2> adj((size_t)medges);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hi, ints.p, sizeof(hi), cudaMemcpyDeviceToHost, g.st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(rp32.data(), G->d_rp, sizeof(int32_t) * rp32.size(), cudaMemcpyDeviceToHost, g.st);
+    if (e == cudaSuccess && medges > 0)
+        e = cudaMemcpyAsync(adj.data(), G->d_adj, sizeof(int2) * adj.size(), cudaMemcpyDeviceToHost, g.st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(g.st);
+    if (e != cudaSuccess) { drop(); return fail(FBC_ERR_CUDA, std::string("graph build: ") + cudaGetErrorString(e)); }
+    if (hi[1] & fbc::kGbNonInt) { drop(); return fail(FBC_ERR_RANGE, "edge weights must be integers below 2^31"); }
+    unsigned long long sumw = 0;
+    std::memcpy(&sumw, hi + 4, sizeof(sumw));
+    G->m = medges;
+    G->maxw = hi[2];
+    G->maxindeg = hi[3];
+    G->meanw = medges ? (double)sumw / (double)medges : 1.0;
+    if ((double)n * (double)G->maxw > 2147483646.0) {
+        drop();
+        return fail(FBC_ERR_RANGE, "n * max_weight exceeds the int32 distance range");
+    }
+    G->h_rp.resize((size_t)n + 1);
+    for (int32_t v = 0; v <= n; ++v) G->h_rp[v] = rp32[v];
+    G->h_col.resize((size_t)medges);
+    G->h_w.resize((size_t)medges);
+    for (int32_t k = 0; k < medges; ++k) {
+        G->h_col[k] = adj[k].x;
+        G->h_w[k] = adj[k].y;
+    }
+    *out = guard.release();
+    return FBC_OK;
+}
+
 }  // namespace
 
 // Error text of the calling thread, shared with the other translation units of the library.
@@ -1036,6 +1156,7 @@ int fbc_set_option(const char* key, int64_t value) {
     else if (k == "iter_mult") g.opt.iter_mult = std::max<int64_t>(1, std::min<int64_t>(1 << 20, value));
     else if (k == "ws_budget_mb") g.opt.ws_budget_mb = std::max<int64_t>(0, value);
     else if (k == "order_min_n") g.opt.order_min_n = std::max<int64_t>(0, value);
+    else if (k == "csr_device_min_m") g.opt.csr_device_min_m = std::max<int64_t>(0, value);
     else if (k == "group") {
         if (value != 0 && value != 1 && value != 2 && value != 4) return fail(FBC_ERR_INVALID_ARG, "group must be 0, 1, 2 or 4");
         g.opt.group = value;
@@ -1060,6 +1181,7 @@ int fbc_get_option(const char* key, int64_t* value) {
     else if (k == "ws_budget_mb") *value = g.opt.ws_budget_mb;
     else if (k == "group") *value = g.opt.group;
     else if (k == "order_min_n") *value = g.opt.order_min_n;
+    else if (k == "csr_device_min_m") *value = g.opt.csr_device_min_m;
     else if (k == "warp_smem") *value = g.opt.warp_smem;
     else if (k == "debug_sched") *value = g.opt.debug_sched;
     else return fail(FBC_ERR_INVALID_ARG, "unknown option " + k);
@@ -1087,6 +1209,10 @@ int fbc_graph_from_edges(int64_t count, const int32_t* src, const int32_t* dst, 
     if (!out || count < 0 || (count > 0 && (!src || !dst || !w)))
         return fail(FBC_ERR_INVALID_ARG, "null argument");
     *out = nullptr;
+    if (count >= g.opt.csr_device_min_m && count < ((int64_t)1 << 31) - 1) {
+        FBC_TRY(device_graph_from_edges(count, src, dst, w, out));
+        if (*out) return FBC_OK;  // else a row too long for the device sort: the host path
+    }
     int32_t maxs = -1;
     for (int64_t i = 0; i < count; ++i) {
         if (!(w[i] > 0)) return fail(FBC_ERR_INVALID_ARG, "Edge weight must be greater than zero");
