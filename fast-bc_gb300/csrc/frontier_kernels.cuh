@@ -24,20 +24,24 @@
 
 namespace fbc {
 
-// A queued vertex with what the next step needs, so the step starts with its adjacency
-// loads instead of re-reading the row offsets.
+// A queued entry with its row start, so the step issues its adjacency loads at once (the
+// row end comes from the small, L2-resident row offsets, loaded alongside).
 struct QEnt {
-    int v, e0, deg, pad;
+    int v, e0;
 };
-// A vertex of a Kahn level: distance, row start, final path count, and `dm`: the mask of its
-// tight out-edges found by the counting sweep (bit k: edge e0 + k), so that the Kahn and
-// dependency passes touch only those; all ones for rows longer than 32 edges (then every edge
-// of the row is re-tested).
+// A Kahn-level entry: row start and (final path count << 16 | tight-edge mask).  The mask is the
+// vertex's tight out-edges found by the counting sweep (bit k: edge e0 + k), so that the Kahn
+// and dependency passes touch only those; kLongRow for rows of more than 15 edges (then every
+// edge of the row is re-tested against the distances).  Path counts are below 2^48 here.
 struct LEnt {
-    int v, d, e0;
-    unsigned dm;
-    unsigned long long sig;
+    int v, e0;
+    unsigned long long sigdm;
 };
+constexpr unsigned kLongRow = 0xffffu;
+constexpr int kMaskEdges = 15;
+__device__ __forceinline__ unsigned long long sig_dm(unsigned long long sig, unsigned mask) {
+    return (sig << 16) | (mask == 0xffffffffu ? kLongRow : (mask & kLongRow));
+}
 
 // Near queues and far piles hold a vertex at most once each, but the frontiers of road-like
 // graphs are far smaller than n: they get qcap entries, and a unit that would overflow them is
@@ -171,8 +175,7 @@ __device__ void frontier_group(const KParams& P, const Unit* us, const FState<Pr
             const int src = us[k].src;
             if (src < 0) continue;
             S.word[src * K + k] = 0ull;  // dist 0, stamp 0
-            const int e0 = __ldg(rp + src);
-            S.q[0][c++] = QEnt{src * K + k, e0, __ldg(rp + src + 1) - e0, 0};
+            S.q[0][c++] = QEnt{src * K + k, __ldg(rp + src)};
         }
         C.ncnt[0] = c;
         C.ncnt[1] = 0;
@@ -203,7 +206,7 @@ __device__ void frontier_group(const KParams& P, const Unit* us, const FState<Pr
                     if (i < ncur) {
                         const QEnt q = qc[i];
                         e[j] = q.e0;
-                        e1[j] = q.e0 + q.deg;
+                        e1[j] = __ldg(rp + (q.v >> kSh) + 1);
                         kk[j] = q.v & (K - 1);
                         dv[j] = dist_of(ldcg64(S.word + q.v));  // may have dropped since the push
                     }
@@ -213,7 +216,7 @@ __device__ void frontier_group(const KParams& P, const Unit* us, const FState<Pr
 #pragma unroll
                     for (int j = 0; j < kE; ++j) more |= e[j] < e1[j];
                     if (!__any_sync(kFull, more)) break;
-                    int x[kE * 4], nd[kE * 4], r0[kE * 4], r1[kE * 4];
+                    int x[kE * 4], nd[kE * 4], r0[kE * 4];
                     unsigned long long old[kE * 4];
 #pragma unroll
                     for (int t = 0; t < kE * 4; ++t) {
@@ -224,7 +227,6 @@ __device__ void frontier_group(const KParams& P, const Unit* us, const FState<Pr
                             x[t] = (a.x << kSh) + kk[j];
                             nd[t] = dv[j] + a.y;
                             r0[t] = __ldg(rp + a.x);  // x's row, in flight with the atomic
-                            r1[t] = __ldg(rp + a.x + 1);
                         }
                     }
 #pragma unroll
@@ -242,7 +244,7 @@ __device__ void frontier_group(const KParams& P, const Unit* us, const FState<Pr
                                 pf = !near;
                             }
                         }
-                        const QEnt qe{x[t], r0[t], r1[t] - r0[t], 0};
+                        const QEnt qe{x[t], r0[t]};
                         bpush(pn, qe, qnx, &C.ncnt[qs ^ 1], qc_cap, &C.ovf);
                         bpush(pf, qe, qfx, &C.fcnt[fs], qc_cap, &C.ovf);
                     }
@@ -280,7 +282,7 @@ __device__ void frontier_group(const KParams& P, const Unit* us, const FState<Pr
         for (int base = tid & ~31; base < nfar; base += nth) {
             const int i = base + (tid & 31);
             bool pn = false, pf = false;
-            QEnt qe{0, 0, 0, 0};
+            QEnt qe{0, 0};
             if (i < nfar) {
                 qe = qfc[i];
                 const int d = dist_of(ldcg64(S.word + qe.v));
@@ -352,7 +354,7 @@ __device__ void frontier_group(const KParams& P, const Unit* us, const FState<Pr
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
                 const int vk = v0 + j * nth;
-                if (vk < nK && dv[j] != kInf) S.rec[vk].mask = e1[j] - eb[j] > 32 ? 0xffffffffu : mk[j];
+                if (vk < nK && dv[j] != kInf) S.rec[vk].mask = e1[j] - eb[j] > kMaskEdges ? 0xffffffffu : mk[j];
             }
         }
         __syncthreads();
@@ -361,7 +363,7 @@ __device__ void frontier_group(const KParams& P, const Unit* us, const FState<Pr
             for (int k = 0; k < K; ++k) {
                 const int src = us[k].src;
                 if (src < 0) continue;
-                S.order[c++] = LEnt{src * K + k, 0, __ldg(rp + src), __ldcg(&S.rec[src * K + k].mask), 1ull};
+                S.order[c++] = LEnt{src * K + k, __ldg(rp + src), sig_dm(1ull, __ldcg(&S.rec[src * K + k].mask))};
             }
             S.lvl[0] = 0;
             C.ocnt = c;
@@ -386,12 +388,12 @@ __device__ void frontier_group(const KParams& P, const Unit* us, const FState<Pr
                     sv[j] = 0ull;
                     if (i < hi) {
                         const LEnt o = S.order[i];
-                        dv[j] = o.d;
-                        sv[j] = o.sig;
+                        sv[j] = o.sigdm >> 16;
                         e0[j] = o.e0;
-                        mk[j] = o.dm;
+                        mk[j] = (unsigned)(o.sigdm & kLongRow);
                         kk[j] = o.v & (K - 1);
-                        if (mk[j] == 0xffffffffu) {  // long row: walk it and re-test every edge
+                        if (mk[j] == kLongRow) {  // long row: walk it and re-test every edge
+                            dv[j] = dist_of(ldcg64(S.word + o.v));
                             e[j] = o.e0;
                             e1[j] = __ldg(rp + (o.v >> kSh) + 1);
                             mk[j] = 0u;
@@ -440,14 +442,13 @@ __device__ void frontier_group(const KParams& P, const Unit* us, const FState<Pr
 #pragma unroll
                     for (int j = 0; j < kV; ++j) {
                         bool push = false;
-                        LEnt le{x[j], nd[j], 0, 0u, 0ull};
+                        LEnt le{x[j], 0, 0ull};
                         if (tight[j]) {
                             const unsigned long long sx = (old[j] >> 16) + sv[j];
                             if (sx > kSigMax || sv[j] > kSigMax) bad |= kErrRetry;
                             push = (old[j] & 0xffffull) == 1ull;
-                            le.sig = sx;
                             le.e0 = r0[j];
-                            le.dm = tm[j];
+                            le.sigdm = sig_dm(sx, tm[j]);
                         }
                         bpush(push, le, S.order, &C.ocnt, (int)cap + 1, &C.ovf);
                     }
@@ -496,7 +497,8 @@ __device__ void frontier_group(const KParams& P, const Unit* us, const FState<Pr
                     mk[j] = 0u;
                     if (i < a1) {
                         o[j] = S.order[i];
-                        mk[j] = o[j].dm == 0xffffffffu ? 0u : o[j].dm;
+                        mk[j] = (unsigned)(o[j].sigdm & kLongRow);
+                        if (mk[j] == kLongRow) mk[j] = 0u;
                     }
                 }
                 for (;;) {
@@ -526,25 +528,28 @@ __device__ void frontier_group(const KParams& P, const Unit* us, const FState<Pr
 #pragma unroll
                     for (int j = 0; j < kV; ++j)
                         if (x[j] >= 0) {
-                            if (sx[j] == o[j].sig) Prec::add_same(acc[j], dx[j]);
-                            else Prec::add(acc[j], o[j].sig, sx[j], dx[j]);
+                            const unsigned long long sv = o[j].sigdm >> 16;
+                            if (sx[j] == sv) Prec::add_same(acc[j], dx[j]);
+                            else Prec::add(acc[j], sv, sx[j], dx[j]);
                         }
                 }
 #pragma unroll
                 for (int j = 0; j < kV; ++j) {
                     if (o[j].v < 0) continue;
                     const int v = o[j].v >> kSh, k = o[j].v & (K - 1);
-                    if (o[j].dm == 0xffffffffu) {  // long row: re-test every edge
+                    if ((o[j].sigdm & kLongRow) == kLongRow) {  // long row: re-test every edge
                         const int e1 = __ldg(rp + v + 1);
+                        const int dv = dist_of(ldcg64(S.word + o[j].v));
+                        const unsigned long long sv = o[j].sigdm >> 16;
                         for (int e = o[j].e0; e < e1; ++e) {
                             const int2 a = __ldg(adj + e);
                             const int xk = (a.x << kSh) + k;
-                            if (o[j].d + a.y == dist_of(ldcg64(S.word + xk))) {
+                            if (dv + a.y == dist_of(ldcg64(S.word + xk))) {
                                 const ulonglong2 r = __ldcg(reinterpret_cast<const ulonglong2*>(S.rec + xk));
                                 const unsigned long long s2 = r.x >> 16;
                                 const typename Prec::D d2 = bits_to<typename Prec::D>(r.y);
-                                if (s2 == o[j].sig) Prec::add_same(acc[j], d2);
-                                else Prec::add(acc[j], o[j].sig, s2, d2);
+                                if (s2 == sv) Prec::add_same(acc[j], d2);
+                                else Prec::add(acc[j], sv, s2, d2);
                             }
                         }
                     }
