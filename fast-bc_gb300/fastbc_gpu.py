@@ -285,15 +285,25 @@ class ClusterEval:
 
 
 def cluster_eval_batch(g: Graph, cs: ClusterSet, precision: int = FP64, sched: int = PLAIN,
-                       intra_bc: np.ndarray | None = None, stats: Stats | None = None) -> ClusterEval:
+                       intra_bc: np.ndarray | None = None, stats: Stats | None = None,
+                       out: "ClusterEval | None" = None) -> ClusterEval:
+    """Evaluate every cluster (DijkstraClusterEvaluator::evaluateCluster for all of them).
+    `out`: a ClusterEval of an earlier call on the same clusters whose arrays are reused (a
+    repeated sweep then writes into memory that is already mapped); intra_bc is added to."""
     cs = cs.with_borders(g)
     nb = np.diff(cs.boff)
     sizes = np.diff(cs.off)
     entry_off = np.zeros(cs.count + 1, np.int64)
     entry_off[1:] = np.cumsum(nb * sizes)
     ent = int(entry_off[-1])
-    bd = np.zeros(max(ent, 1), np.float64)
-    bs = np.zeros(max(ent, 1), np.uint64)
+    if out is not None and out.border_dist.size == ent and out.border_sigma.size == ent and ent > 0:
+        bd, bs = out.border_dist, out.border_sigma
+        if intra_bc is None:
+            intra_bc = out.intra_bc
+            intra_bc[:] = 0.0
+    else:
+        bd = np.zeros(max(ent, 1), np.float64)
+        bs = np.zeros(max(ent, 1), np.uint64)
     if intra_bc is None:
         intra_bc = np.zeros(max(g.n, 1), np.float64)
     _ck(lib.fbc_cluster_eval_batch(g._h, cs.count, _ptr(cs.off), _ptr(cs.vertices), _ptr(cs.boff),
