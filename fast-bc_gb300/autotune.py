@@ -40,7 +40,7 @@ def _apply(choice: dict) -> dict:
 
 
 def tune_pivots(g: fg.Graph, sources, cards=None, precision: int = fg.FP32C, sample: int = 4096,
-                deltas=(2, 4, 8), threads=(96, 128, 512)) -> dict:
+                deltas=(2, 4, 8), threads=(64, 96, 128, 512)) -> dict:
     """Whole-graph sources (pivots, exact mode): delta (as multiples of the mean weight) and
     the frontier kernel's block size.  Up to `sample` sources the whole list is timed, so the
     number of waves over the concurrent slots (which the block size sets) is the real one."""

@@ -145,9 +145,8 @@ __device__ __forceinline__ void bpush(bool want, const E& x, E* q, int* c, int c
 // of them), and their per-vertex state is interleaved, entry v*K + k for source k, so the
 // words of nearby sources' wavefronts share sectors and the adjacency rows they read are the
 // same.  Queue and level entries name an entry vk = v*K + k.  K = 1 is one source per block.
-// kV: vertices per lane in the Kahn and dependency passes (2 for the wide blocks of
-// million-vertex graphs, whose levels are thousands wide -- 4 measured slower, spilling at the
-// 128-register cap; 1 for the narrow blocks); kE:
+// kV: level entries per lane in the Kahn and dependency passes (2: their loads and atomics are
+// in flight together; 4 measured slower, spilling at the register caps); kE:
 // queued entries per lane in the distance pass (1: two measured slower on the wide blocks,
 // which then spill at their 128-register cap).
 template <class Prec, int kV, int K, int kE>
@@ -615,7 +614,7 @@ __global__ void __launch_bounds__(kWide ? 512 : 128, kWide ? 1 : 5) frontier_ker
         if (gi < P.nunits && threadIdx.x < K) us[threadIdx.x] = P.units[gi * K + threadIdx.x];
         __syncthreads();
         if (gi >= P.nunits) break;
-        frontier_group<Prec, kWide ? 2 : 1, K, 1>(P, us, S, C, cap);
+        frontier_group<Prec, 2, K, 1>(P, us, S, C, cap);
     }
 }
 
