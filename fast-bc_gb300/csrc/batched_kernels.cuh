@@ -12,7 +12,8 @@
 //     vertex's queue stamp de-duplicates pushes (no intra-warp matching needed), path
 //     counts are two 32-bit words with an explicit carry;
 //   * a warp owns a source: queue counters are registers, pushes are ballots, and each lane
-//     walks the adjacency of one queued vertex (road-like graphs have degree <= ~6);
+//     walks the adjacency of one queued vertex (road-like graphs have degree <= ~6), four
+//     edges at a time so that their shared-memory loads and atomics overlap;
 //   * per-vertex state is 24 bytes: dist (4) + sigma (8) + three 4-byte planes reused per
 //     pass (queues + stamps -> counters/order/levels -> delta/order/levels);
 //   * the warps of a block adapt to the chunk's segment size: as many as its state fits;
@@ -147,23 +148,38 @@ __device__ void small_unit(const KParams& K, const Seg& sg, const Unit& u, const
                     e1 = (int)rp[v + 1];
                 }
                 while (__any_sync(kFull, e < e1)) {
-                    bool pn = false, pf = false;
-                    int x = 0;
-                    if (e < e1) {
-                        const uint32_t a = adj[e++];
-                        x = (int)(a & 0xffffu);
-                        const int nd = dv + (int)(a >> 16);
-                        if (nd < atomicMin(dist + x, nd)) {
-                            const bool near = nd < T;
-                            const unsigned s = near ? nst : fst;
-                            if (atomicExch(stamp_of + x, s) != s) {
-                                pn = near;
-                                pf = !near;
-                            }
+                    // up to four edges of the lane's vertex at once: their atomics overlap
+                    int x[4], nd[4], od[4];
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) {
+                        x[k] = -1;
+                        if (e + k < e1) {
+                            const uint32_t a = adj[e + k];
+                            x[k] = (int)(a & 0xffffu);
+                            nd[k] = dv + (int)(a >> 16);
                         }
                     }
-                    wpush16(pn, x, qnx, nnext);
-                    wpush16(pf, x, qfx, nfar);
+#pragma unroll
+                    for (int k = 0; k < 4; ++k)
+                        if (x[k] >= 0) od[k] = atomicMin(dist + x[k], nd[k]);
+                    unsigned os[4], sk[4];
+#pragma unroll
+                    for (int k = 0; k < 4; ++k)
+                        if (x[k] >= 0 && nd[k] < od[k]) {
+                            sk[k] = nd[k] < T ? nst : fst;
+                            os[k] = atomicExch(stamp_of + x[k], sk[k]);
+                        }
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) {
+                        bool pn = false, pf = false;
+                        if (x[k] >= 0 && nd[k] < od[k] && os[k] != sk[k]) {
+                            pn = nd[k] < T;
+                            pf = !pn;
+                        }
+                        wpush16(pn, x[k], qnx, nnext);
+                        wpush16(pf, x[k], qfx, nfar);
+                    }
+                    e += 4;
                 }
             }
             __syncwarp();
@@ -224,10 +240,23 @@ __device__ void small_unit(const KParams& K, const Seg& sg, const Unit& u, const
                 const int dv = dist[v];
                 if (dv != kInf) {
                     const int e1 = (int)rp[v + 1];
-                    for (int e = (int)rp[v]; e < e1; ++e) {
-                        const uint32_t a = adj[e];
-                        const int x = (int)(a & 0xffffu);
-                        if (dv + (int)(a >> 16) == dist[x]) atomicAdd(cnt + x, 1u);
+                    for (int e = (int)rp[v]; e < e1; e += 4) {
+                        int x[4], dx[4], nd[4];
+#pragma unroll
+                        for (int k = 0; k < 4; ++k) {
+                            x[k] = -1;
+                            if (e + k < e1) {
+                                const uint32_t a = adj[e + k];
+                                x[k] = (int)(a & 0xffffu);
+                                nd[k] = dv + (int)(a >> 16);
+                            }
+                        }
+#pragma unroll
+                        for (int k = 0; k < 4; ++k)
+                            if (x[k] >= 0) dx[k] = dist[x[k]];
+#pragma unroll
+                        for (int k = 0; k < 4; ++k)
+                            if (x[k] >= 0 && nd[k] == dx[k]) atomicAdd(cnt + x[k], 1u);
                     }
                 }
             }
@@ -254,17 +283,31 @@ __device__ void small_unit(const KParams& K, const Seg& sg, const Unit& u, const
                     e1 = (int)rp[v + 1];
                 }
                 while (__any_sync(kFull, e < e1)) {
-                    bool push = false;
-                    int x = 0;
-                    if (e < e1) {
-                        const uint32_t a = adj[e++];
-                        x = (int)(a & 0xffffu);
-                        if (dv + (int)(a >> 16) == dist[x]) {
-                            if (sig_add(slo, shi, x, sv)) bad |= kErrSigma;
-                            push = atomicSub(cnt + x, 1u) == 1u;
+                    int x[4], nd[4], dx[4];
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) {
+                        x[k] = -1;
+                        if (e + k < e1) {
+                            const uint32_t a = adj[e + k];
+                            x[k] = (int)(a & 0xffffu);
+                            nd[k] = dv + (int)(a >> 16);
                         }
                     }
-                    wpush16(push, x, order, nxt);
+#pragma unroll
+                    for (int k = 0; k < 4; ++k)
+                        if (x[k] >= 0) dx[k] = dist[x[k]];
+                    bool push[4];
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) {
+                        push[k] = false;
+                        if (x[k] >= 0 && nd[k] == dx[k]) {
+                            if (sig_add(slo, shi, x[k], sv)) bad |= kErrSigma;
+                            push[k] = atomicSub(cnt + x[k], 1u) == 1u;
+                        }
+                    }
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) wpush16(push[k], x[k], order, nxt);
+                    e += 4;
                 }
             }
             __syncwarp();
@@ -295,14 +338,27 @@ __device__ void small_unit(const KParams& K, const Seg& sg, const Unit& u, const
                 const unsigned long long sv = sig_get(slo, shi, v);
                 typename Prec::Acc acc = Prec::zero();
                 const int e1 = (int)rp[v + 1];
-                for (int e = (int)rp[v]; e < e1; ++e) {
-                    const uint32_t a = adj[e];
-                    const int x = (int)(a & 0xffffu);
-                    if (dv + (int)(a >> 16) == dist[x]) {
-                        const unsigned long long sx = sig_get(slo, shi, x);
-                        if (sx == sv) Prec::add_same(acc, dlt[x]);
-                        else Prec::add(acc, sv, sx, dlt[x]);
+                for (int e = (int)rp[v]; e < e1; e += 4) {
+                    int x[4];
+                    bool tight[4];
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) {
+                        x[k] = -1;
+                        tight[k] = false;
+                        if (e + k < e1) {
+                            const uint32_t a = adj[e + k];
+                            x[k] = (int)(a & 0xffffu);
+                            tight[k] = dv + (int)(a >> 16) == dist[x[k]];
+                        }
                     }
+                    // accumulate in adjacency order (deterministic)
+#pragma unroll
+                    for (int k = 0; k < 4; ++k)
+                        if (tight[k]) {
+                            const unsigned long long sx = sig_get(slo, shi, x[k]);
+                            if (sx == sv) Prec::add_same(acc, dlt[x[k]]);
+                            else Prec::add(acc, sv, sx, dlt[x[k]]);
+                        }
                 }
                 dlt[v] = Prec::store(acc);
                 if (v != src) {
