@@ -667,7 +667,27 @@ int run_plan_t(Plan& P, fbc_stats* st) {
     FBC_CK(g.retry.ensure(sizeof(fbc::RetryRec) * std::max<size_t>(P.units.size(), 1)));
     FBC_TRY(launch_small<Prec>(P, uw, nw_max, mw_max, nw_min, st, launches));
     FBC_CK(cudaEventRecord(g.evm, g.st));
-    FBC_TRY(launch_block<Prec>(P, ub, nb_max, st, launches));
+    {
+        // batched: segments of up to 32K vertices run in a launch of their own (where several
+        // sources share a block, their rounds and levels), the larger ones one source per block
+        std::vector<Unit> us_small, us_large;
+        int ns_max = 0, nl_max = 0;
+        if (P.sched == FBC_SCHED_BATCHED && !P.dbg_dist)
+            for (const Unit& u : ub) {
+                const int sn = P.segs[u.seg].n;
+                if (sn <= 32768) { us_small.push_back(u); ns_max = std::max(ns_max, sn); }
+                else { us_large.push_back(u); nl_max = std::max(nl_max, sn); }
+            }
+        if (!us_small.empty() && !us_large.empty()) {
+            // the launch with the larger slot layout first, so that the second reuses it
+            const bool small_first = (int64_t)ns_max * 4 >= (int64_t)nl_max;
+            FBC_TRY(launch_block<Prec>(P, small_first ? us_small : us_large, small_first ? ns_max : nl_max, st, launches));
+            FBC_CK(cudaMemsetAsync(g.ctr.p, 0, 8, g.st));  // the unit counter of the next launch
+            FBC_TRY(launch_block<Prec>(P, small_first ? us_large : us_small, small_first ? nl_max : ns_max, st, launches));
+        } else {
+            FBC_TRY(launch_block<Prec>(P, ub, nb_max, st, launches));
+        }
+    }
     int err[2] = {0, 0};
     FBC_CK(cudaMemcpyAsync(err, (char*)g.ctr.p + 16, 2 * sizeof(int), cudaMemcpyDeviceToHost, g.st));
     FBC_CK(cudaStreamSynchronize(g.st));
@@ -676,6 +696,7 @@ int run_plan_t(Plan& P, fbc_stats* st) {
     // 48-bit packed -> 64-bit (plain kernel) -> FP64 counts (plain kernel).
     for (int round = 0; round < 3 && err[0] == 0 && err[1] > 0; ++round) {
         std::vector<fbc::RetryRec> rec((size_t)err[1]);
+        if (st) st->retries += err[1];
         FBC_CK(cudaMemcpy(rec.data(), g.retry.p, sizeof(fbc::RetryRec) * rec.size(), cudaMemcpyDeviceToHost));
         std::vector<Unit> to64, tof64;
         int nmax = 0;

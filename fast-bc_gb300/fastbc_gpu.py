@@ -54,7 +54,7 @@ class Stats(C.Structure):
                 ("launches", C.c_int32), ("slots", C.c_int32), ("warp_ms", C.c_double),
                 ("block_ms", C.c_double), ("warp_bytes", C.c_double), ("block_bytes", C.c_double),
                 ("warp_units", C.c_int64), ("block_units", C.c_int64), ("group", C.c_int32),
-                ("pad", C.c_int32)]
+                ("retries", C.c_int32)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}

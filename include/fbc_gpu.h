@@ -69,7 +69,7 @@ typedef struct {
     int64_t warp_units;
     int64_t block_units;
     int32_t group;           /* sources per block of the frontier kernel (0: not launched)  */
-    int32_t pad;
+    int32_t retries;         /* units recomputed by the plain kernel with wider path counts */
 } fbc_stats;
 
 /* Library lifetime.  fbc_gpu_init selects the device and creates the library stream. */

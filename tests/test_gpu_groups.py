@@ -101,3 +101,19 @@ def test_grid2048_grouped_matches_single(fg, group):
     c = fg.dependency_batch(g, src, None, fg.FP64, fg.BATCHED)
     assert rel_err(a, c) <= TOL_FP64
     assert rel_err(b, c) <= TOL_FP32C
+
+
+def test_mixed_segment_sizes_split_launches(fg):
+    """A batch with graphs on both sides of the 32K-vertex line runs as two frontier launches
+    (grouped small segments, then one source per block): every graph's exact BC equals its
+    single-graph run."""
+    els = [graphs.rgg_knn(n, seed=17, gid=i) for i, n in enumerate([6000, 33000, 9000])]
+    gs = [fg.Graph.from_edgelist(e) for e in els]
+    old = fg.get_option("warp_max_n")
+    fg.set_option("warp_max_n", 0)  # every graph on the frontier kernel
+    try:
+        outs = fg.multi_exact_bc(gs, fg.FP64, fg.BATCHED)
+        for gr, o in zip(gs, outs):
+            assert rel_err(o, fg.exact_bc(gr, fg.FP64, fg.BATCHED)) <= TOL_FP64
+    finally:
+        fg.set_option("warp_max_n", old)
