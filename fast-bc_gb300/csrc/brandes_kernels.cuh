@@ -89,6 +89,7 @@ struct KParams {
     int* retry_count;            // units to recompute one level up (null: report an error)
     RetryRec* retry;
     int32_t retry_cap;
+    int32_t cnt_bits;            // frontier kernel: counter / mask bits next to the path count
     int32_t* dbg_dist;           // debug dump of one unit (may be null)
     unsigned long long* dbg_sig;
     double* dbg_dlt;

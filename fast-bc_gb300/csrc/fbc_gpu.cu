@@ -499,6 +499,13 @@ int launch_block(const Plan& P, const std::vector<Unit>& units_in, int ws_n, fbc
     KParams K = base_params(P);
     K.units = g.units_b.as<Unit>();
     K.nunits = (int64_t)units.size() / Kg;
+    if (fr) {
+        // 8-bit counters (path counts up to 2^56) when no vertex of the launch's segments has
+        // 255 or more in-edges, else 16-bit (the host keeps segments of 65,535+ off this kernel)
+        int32_t maxin = 0;
+        for (const Unit& u : units) maxin = std::max(maxin, P.seg_maxindeg[u.seg]);
+        K.cnt_bits = maxin < 255 ? 8 : 16;
+    }
     K.next_unit = g.ctr.as<unsigned long long>() + 0;
     K.ws = W.buf.as<char>();
     K.ws_stride = W.stride;

@@ -10,7 +10,8 @@
 //   * queue entries carry the vertex's row (loaded from the small, L2-resident row offsets
 //     alongside the atomic that pushed it) and Kahn-level entries carry distance, row, final
 //     path count and tight-edge mask, so a step starts with its adjacency loads;
-//   * path count and Kahn counter share one 64-bit word (sigma << 16 | counter), so one atomic
+//   * path count and Kahn counter share one 64-bit word (sigma << B | counter; B = 8 bits when
+//     no vertex has 255 or more in-edges, else 16), so one atomic
 //     both adds sigma_v and retires the edge, and the thread that retires the last tight
 //     in-edge learns the final count; the word sits in a 16-byte record with the dependency
 //     (which holds the tight-edge mask until the dependency pass), so a Kahn push and a
@@ -29,19 +30,26 @@ namespace fbc {
 struct QEnt {
     int v, e0;
 };
-// A Kahn-level entry: row start and (final path count << 16 | tight-edge mask).  The mask is the
-// vertex's tight out-edges found by the counting sweep (bit k: edge e0 + k), so that the Kahn
-// and dependency passes touch only those; kLongRow for rows of more than 15 edges (then every
-// edge of the row is re-tested against the distances).  Path counts are below 2^48 here.
+// A Kahn-level entry: row start and (final path count << B | tight-edge mask), B the launch's
+// field width (8 or 16 bits).  The mask is the vertex's tight out-edges found by the counting
+// sweep (bit k: edge e0 + k), so that the Kahn and dependency passes touch only those; all B
+// bits set (the long-row mark) for rows of B or more edges (then every edge of the row is
+// re-tested against the distances).  Path counts are below 2^(64 - B) here.
 struct LEnt {
     int v, e0;
     unsigned long long sigdm;
 };
-constexpr unsigned kLongRow = 0xffffu;
-constexpr int kMaskEdges = 15;
-__device__ __forceinline__ unsigned long long sig_dm(unsigned long long sig, unsigned mask) {
-    return (sig << 16) | (mask == 0xffffffffu ? kLongRow : (mask & kLongRow));
-}
+// the packed fields of one launch: B = cb bits of counter / mask next to the path count
+struct Packing {
+    int cb;
+    unsigned long long low;      // (1 << cb) - 1: counter mask, long-row mark
+    unsigned long long sigmax;   // 2^(64 - cb) - 1
+    __device__ explicit Packing(int bits)
+        : cb(bits), low((1ull << bits) - 1ull), sigmax((1ull << (64 - bits)) - 1ull) {}
+    __device__ unsigned long long sig_dm(unsigned long long sig, unsigned mask) const {
+        return (sig << cb) | (mask == 0xffffffffu ? low : ((unsigned long long)mask & low));
+    }
+};
 
 // Near queues and far piles hold a vertex at most once each, but the frontiers of road-like
 // graphs are far smaller than n: they get qcap entries, and a unit that would overflow them is
@@ -57,7 +65,7 @@ __host__ __device__ inline int64_t fqcap(int64_t cap) {
 // so the Kahn pass finds a released vertex's mask in the sector its count atomic just touched.
 template <class Prec>
 struct __align__(16) FRec {
-    unsigned long long sc;        // (sigma << 16 | tight in-edges still unprocessed)
+    unsigned long long sc;        // (sigma << B | tight in-edges still unprocessed)
     union {
         typename Prec::D dlt;
         unsigned mask;
@@ -102,9 +110,8 @@ struct FCtl {
     int ovf;   // a queue push did not fit
 };
 
-// Path counts share a word with the counter, so they are limited to 2^48 - 1 here; a unit
-// that exceeds it stops before its dependency pass and is recomputed by the plain kernel.
-constexpr unsigned long long kSigMax = (1ull << 48) - 1ull;
+// Path counts share a word with the counter, so they are limited to 2^(64 - B) - 1 here; a
+// unit that exceeds it stops before its dependency pass and is recomputed by the plain kernel.
 
 __device__ __forceinline__ unsigned long long ldcg64(const unsigned long long* p) { return __ldcg(p); }
 
@@ -162,6 +169,8 @@ __device__ void frontier_group(const KParams& P, const Unit* us, const FState<Pr
     const int delta = sg.delta > 0 ? sg.delta : 1;
     const int tid = threadIdx.x, nth = blockDim.x;
     const int qc_cap = (int)fqcap(cap);
+    const Packing pk(P.cnt_bits);
+    const int mask_edges = pk.cb - 1;  // rows of more edges carry the long-row mark
     int bad = 0;
 
     // ---------------------------------------------------------------- distances
@@ -353,7 +362,7 @@ __device__ void frontier_group(const KParams& P, const Unit* us, const FState<Pr
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
                 const int vk = v0 + j * nth;
-                if (vk < nK && dv[j] != kInf) S.rec[vk].mask = e1[j] - eb[j] > kMaskEdges ? 0xffffffffu : mk[j];
+                if (vk < nK && dv[j] != kInf) S.rec[vk].mask = e1[j] - eb[j] > mask_edges ? 0xffffffffu : mk[j];
             }
         }
         __syncthreads();
@@ -362,7 +371,7 @@ __device__ void frontier_group(const KParams& P, const Unit* us, const FState<Pr
             for (int k = 0; k < K; ++k) {
                 const int src = us[k].src;
                 if (src < 0) continue;
-                S.order[c++] = LEnt{src * K + k, __ldg(rp + src), sig_dm(1ull, __ldcg(&S.rec[src * K + k].mask))};
+                S.order[c++] = LEnt{src * K + k, __ldg(rp + src), pk.sig_dm(1ull, __ldcg(&S.rec[src * K + k].mask))};
             }
             S.lvl[0] = 0;
             C.ocnt = c;
@@ -387,11 +396,11 @@ __device__ void frontier_group(const KParams& P, const Unit* us, const FState<Pr
                     sv[j] = 0ull;
                     if (i < hi) {
                         const LEnt o = S.order[i];
-                        sv[j] = o.sigdm >> 16;
+                        sv[j] = o.sigdm >> pk.cb;
                         e0[j] = o.e0;
-                        mk[j] = (unsigned)(o.sigdm & kLongRow);
+                        mk[j] = (unsigned)(o.sigdm & pk.low);
                         kk[j] = o.v & (K - 1);
-                        if (mk[j] == kLongRow) {  // long row: walk it and re-test every edge
+                        if (mk[j] == (unsigned)pk.low) {  // long row: walk it and re-test every edge
                             dv[j] = dist_of(ldcg64(S.word + o.v));
                             e[j] = o.e0;
                             e1[j] = __ldg(rp + (o.v >> kSh) + 1);
@@ -435,7 +444,7 @@ __device__ void frontier_group(const KParams& P, const Unit* us, const FState<Pr
                         if (tight[j]) {
                             // one atomic adds sigma_v and retires the edge; the thread that
                             // retires the last tight in-edge knows x's final count
-                            old[j] = atomicAdd(&S.rec[x[j]].sc, (sv[j] << 16) - 1ull);
+                            old[j] = atomicAdd(&S.rec[x[j]].sc, (sv[j] << pk.cb) - 1ull);
                             tm[j] = __ldcg(&S.rec[x[j]].mask);  // same sector as the atomic
                         }
 #pragma unroll
@@ -443,11 +452,11 @@ __device__ void frontier_group(const KParams& P, const Unit* us, const FState<Pr
                         bool push = false;
                         LEnt le{x[j], 0, 0ull};
                         if (tight[j]) {
-                            const unsigned long long sx = (old[j] >> 16) + sv[j];
-                            if (sx > kSigMax || sv[j] > kSigMax) bad |= kErrRetry;
-                            push = (old[j] & 0xffffull) == 1ull;
+                            const unsigned long long sx = (old[j] >> pk.cb) + sv[j];
+                            if (sx > pk.sigmax || sv[j] > pk.sigmax) bad |= kErrRetry;
+                            push = (old[j] & pk.low) == 1ull;
                             le.e0 = r0[j];
-                            le.sigdm = sig_dm(sx, tm[j]);
+                            le.sigdm = pk.sig_dm(sx, tm[j]);
                         }
                         bpush(push, le, S.order, &C.ocnt, (int)cap + 1, &C.ovf);
                     }
@@ -474,7 +483,7 @@ __device__ void frontier_group(const KParams& P, const Unit* us, const FState<Pr
                     const int b = sg.border[j] * K + k;
                     const int d = dist_of(ldcg64(S.word + b));
                     P.bdist[u.bout + j] = d != kInf ? (double)d : 0.0;
-                    P.bsig[u.bout + j] = d != kInf ? (d == 0 ? 1ull : __ldcg(&S.rec[b].sc) >> 16) : 0ull;
+                    P.bsig[u.bout + j] = d != kInf ? (d == 0 ? 1ull : __ldcg(&S.rec[b].sc) >> pk.cb) : 0ull;
                 }
             }
         }
@@ -496,8 +505,8 @@ __device__ void frontier_group(const KParams& P, const Unit* us, const FState<Pr
                     mk[j] = 0u;
                     if (i < a1) {
                         o[j] = S.order[i];
-                        mk[j] = (unsigned)(o[j].sigdm & kLongRow);
-                        if (mk[j] == kLongRow) mk[j] = 0u;
+                        mk[j] = (unsigned)(o[j].sigdm & pk.low);
+                        if (mk[j] == (unsigned)pk.low) mk[j] = 0u;
                     }
                 }
                 for (;;) {
@@ -521,13 +530,13 @@ __device__ void frontier_group(const KParams& P, const Unit* us, const FState<Pr
                     for (int j = 0; j < kV; ++j)
                         if (x[j] >= 0) {
                             const ulonglong2 r = __ldcg(reinterpret_cast<const ulonglong2*>(S.rec + x[j]));
-                            sx[j] = r.x >> 16;
+                            sx[j] = r.x >> pk.cb;
                             dx[j] = bits_to<typename Prec::D>(r.y);
                         }
 #pragma unroll
                     for (int j = 0; j < kV; ++j)
                         if (x[j] >= 0) {
-                            const unsigned long long sv = o[j].sigdm >> 16;
+                            const unsigned long long sv = o[j].sigdm >> pk.cb;
                             if (sx[j] == sv) Prec::add_same(acc[j], dx[j]);
                             else Prec::add(acc[j], sv, sx[j], dx[j]);
                         }
@@ -536,16 +545,16 @@ __device__ void frontier_group(const KParams& P, const Unit* us, const FState<Pr
                 for (int j = 0; j < kV; ++j) {
                     if (o[j].v < 0) continue;
                     const int v = o[j].v >> kSh, k = o[j].v & (K - 1);
-                    if ((o[j].sigdm & kLongRow) == kLongRow) {  // long row: re-test every edge
+                    if ((o[j].sigdm & pk.low) == pk.low) {  // long row: re-test every edge
                         const int e1 = __ldg(rp + v + 1);
                         const int dv = dist_of(ldcg64(S.word + o[j].v));
-                        const unsigned long long sv = o[j].sigdm >> 16;
+                        const unsigned long long sv = o[j].sigdm >> pk.cb;
                         for (int e = o[j].e0; e < e1; ++e) {
                             const int2 a = __ldg(adj + e);
                             const int xk = (a.x << kSh) + k;
                             if (dv + a.y == dist_of(ldcg64(S.word + xk))) {
                                 const ulonglong2 r = __ldcg(reinterpret_cast<const ulonglong2*>(S.rec + xk));
-                                const unsigned long long s2 = r.x >> 16;
+                                const unsigned long long s2 = r.x >> pk.cb;
                                 const typename Prec::D d2 = bits_to<typename Prec::D>(r.y);
                                 if (s2 == sv) Prec::add_same(acc[j], d2);
                                 else Prec::add(acc[j], sv, s2, d2);
@@ -575,7 +584,7 @@ __device__ void frontier_group(const KParams& P, const Unit* us, const FState<Pr
         for (int v = tid; v < n; v += nth) {
             const int d = dist_of(ldcg64(S.word + v * K));
             P.dbg_dist[v] = d != kInf ? d : -1;
-            P.dbg_sig[v] = d != kInf ? (v == src ? 1ull : __ldcg(&S.rec[v * K].sc) >> 16) : 0ull;
+            P.dbg_sig[v] = d != kInf ? (v == src ? 1ull : __ldcg(&S.rec[v * K].sc) >> pk.cb) : 0ull;
             P.dbg_dlt[v] = d != kInf ? Prec::value(Prec::load(S.rec[v * K].dlt)) : 0.0;
         }
     }

@@ -117,3 +117,42 @@ def test_mixed_segment_sizes_split_launches(fg):
             assert rel_err(o, fg.exact_bc(gr, fg.FP64, fg.BATCHED)) <= TOL_FP64
     finally:
         fg.set_option("warp_max_n", old)
+
+
+def _hub_graph(n=2500, hub_in=300, seed=3):
+    """A ring with random weights plus one vertex with `hub_in` in-edges (forces the 16-bit
+    counter layout of the frontier kernel)."""
+    rng = np.random.default_rng(seed)
+    src = list(range(n)) + list(range(1, n))
+    dst = [(i + 1) % n for i in range(n)] + [i - 1 for i in range(1, n)]
+    feeders = rng.choice(np.arange(1, n), hub_in, replace=False)
+    src += list(feeders)
+    dst += [0] * hub_in
+    src += [0] * 5
+    dst += list(rng.choice(np.arange(1, n), 5, replace=False))
+    w = rng.integers(1, 50, len(src)).astype(np.float64)
+    return np.array(src, np.int32), np.array(dst, np.int32), w
+
+
+@pytest.mark.parametrize("kind", ["hub", "dense_rows"])
+def test_counter_layouts(fg, kind):
+    """8-bit counters and masks (rows of 8+ edges re-tested) on a graph with long rows, 16-bit ones
+    on a graph with a 300-in-edge vertex: both equal the oracle."""
+    if kind == "hub":
+        s, d, w = _hub_graph()
+        g = fg.Graph.from_edges(s, d, w)
+        og = oracle.CSR(*g.csr())
+    else:
+        el = graphs.rgg_knn(3000, k=12, seed=21)
+        g = fg.Graph.from_edgelist(el)
+        og = oracle.CSR.from_edgelist(el)
+    src = np.arange(0, g.n, max(1, g.n // 40), dtype=np.int32)[:40]
+    ref = oracle.exact_bc_sources(og, src, threads=8)
+    old = fg.get_option("warp_max_n")
+    fg.set_option("warp_max_n", 0)  # the frontier kernel, not the shared-memory one
+    try:
+        for prec, tol in ((fg.FP64, TOL_FP64), (fg.FP32C, TOL_FP32C)):
+            got = fg.dependency_batch(g, src, None, prec, fg.BATCHED)
+            assert rel_err(got, ref) <= tol
+    finally:
+        fg.set_option("warp_max_n", old)
