@@ -442,14 +442,17 @@ def run_reference(args):
         vals.append(v)
         samples.append(what)
     value = float(np.mean(vals))
-    work = work_per_step(el, z)
+    off, cv, boff, bv, poff, pv, kv, keep = cluster_lists(z)
+    work = work_per_step(el, z, keep)
     line = {"metric": METRIC, "value": value, "unit": "GTEPS", "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": work / (value * 1e9) * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic (seeded road grid; reference partition and pivots)",
-            "config": {"workload": "clustered fast-bc, 256x256 road grid (65,536 vertices)",
-                       "graph_seed": 42, "louvain_seeds": [1, 2, 3, 4], "kfrac": 0.5,
-                       "l2": "n/a (CPU)"},
+            "data": "synthetic (seeded road grid; partition and pivots from the reference's Louvain + k-means)",
+            "config": {"workload": "clustered fast-bc, 256x256 road grid (65,536 vertices, 248,528 edges)",
+                       "graph_seed": 42, "louvain_seeds": [1, 2, 3, 4], "louvain_precision": 0.01,
+                       "kfrac": 0.5, "clusters": len(keep), "pivots": int(pv.size),
+                       "relaxations_per_step": work, "precision": "fp64", "schedule": "cpu",
+                       "l2": "n/a (CPU)", "parallelism": f"{threads} host threads"},
             "impl": "reference",
             "cpu_baseline": {"value": value, "unit": "GTEPS", "cores": threads, "kind": "port",
                              "sample": f"per step: {samples[-1]} (bounded sample, ~{args.ref_budget:.0f} s); "
