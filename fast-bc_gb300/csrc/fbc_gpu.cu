@@ -91,6 +91,7 @@ struct Options {
     int64_t group = 0;          // frontier kernel sources per block (1, 2, 4); 0 = automatic
     int64_t order_min_n = 131072;  // batched runs relabel graphs of at least this many vertices
     int64_t csr_device_min_m = 65536;  // edge lists of at least this many edges are built on the device
+    int64_t wide_threads = 512;        // block size of the wide frontier kernel (<= 512)
     int64_t warp_smem = 1;      // batched: warp state in shared memory when it fits
     int64_t debug_sched = FBC_SCHED_PLAIN;  // schedule used by fbc_sssp_debug
 };
@@ -434,7 +435,7 @@ int launch_block(const Plan& P, const std::vector<Unit>& units_in, int ws_n, fbc
     const bool wide = fr && (g.opt.frontier_threads > 128 || (int64_t)ws_n >= g.opt.wide_n);
     int threads = (int)std::min<int64_t>(std::max<int64_t>(fr ? g.opt.frontier_threads : g.opt.block_threads, 32),
                                          fr ? 128 : 1024);
-    if (wide) threads = 512;
+    if (wide) threads = (int)g.opt.wide_threads;
     threads = (threads / 32) * 32;
     // units sorted so that each segment's units are adjacent (the caller sorts by size)
     std::vector<Unit> sorted(units_in);
@@ -1185,6 +1186,7 @@ int fbc_set_option(const char* key, int64_t value) {
     else if (k == "ws_budget_mb") g.opt.ws_budget_mb = std::max<int64_t>(0, value);
     else if (k == "order_min_n") g.opt.order_min_n = std::max<int64_t>(0, value);
     else if (k == "csr_device_min_m") g.opt.csr_device_min_m = std::max<int64_t>(0, value);
+    else if (k == "wide_threads") g.opt.wide_threads = std::max<int64_t>(64, std::min<int64_t>(512, value / 32 * 32));
     else if (k == "group") {
         if (value != 0 && value != 1 && value != 2 && value != 4) return fail(FBC_ERR_INVALID_ARG, "group must be 0, 1, 2 or 4");
         g.opt.group = value;
@@ -1210,6 +1212,7 @@ int fbc_get_option(const char* key, int64_t* value) {
     else if (k == "group") *value = g.opt.group;
     else if (k == "order_min_n") *value = g.opt.order_min_n;
     else if (k == "csr_device_min_m") *value = g.opt.csr_device_min_m;
+    else if (k == "wide_threads") *value = g.opt.wide_threads;
     else if (k == "warp_smem") *value = g.opt.warp_smem;
     else if (k == "debug_sched") *value = g.opt.debug_sched;
     else return fail(FBC_ERR_INVALID_ARG, "unknown option " + k);
