@@ -108,6 +108,23 @@ class Clocks:
                 "samples": len(sm)}
 
 
+def max_over_ranks(values, dist=None, device="cpu"):
+    """The slowest rank's value of each entry (one all-reduce; identity on one process)."""
+    if dist is None:
+        return [float(v) for v in values]
+    import torch
+
+    t = torch.tensor(values, dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(x) for x in t]
+
+
+def replica_gteps(work_per_step, steps, world, seconds):
+    """Whole-job throughput of `world` independent replicas that each ran `steps` steps of
+    `work_per_step` relaxations, the slowest taking `seconds`."""
+    return work_per_step * steps * world / seconds / 1e9
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -600,14 +617,9 @@ def main():
                  "replay_device_ms": float(np.median(rd)),
                  "per_call_wall_ms": float(np.median(sweep_wall)) if sweep_wall else None}
         plan.free()
-    tot_dev = sum(dev_ms) / 1e3
-    tot_wall = sum(wall_ms) / 1e3
-    if dist:
-        t = torch.tensor([tot_dev, tot_wall], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        tot_dev, tot_wall = float(t[0]), float(t[1])
-    value = work * args.steps * ws / tot_dev / 1e9
-    e2e = work * args.steps * ws / tot_wall / 1e9
+    tot_dev, tot_wall = max_over_ranks([sum(dev_ms) / 1e3, sum(wall_ms) / 1e3], dist, "cuda")
+    value = replica_gteps(work, args.steps, ws, tot_dev)
+    e2e = replica_gteps(work, args.steps, ws, tot_wall)
     if rank != 0:
         if dist:
             dist.destroy_process_group()
