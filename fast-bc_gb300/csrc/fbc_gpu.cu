@@ -1182,7 +1182,7 @@ int fbc_set_option(const char* key, int64_t value) {
     else if (k == "wide_n") g.opt.wide_n = std::max<int64_t>(1, value);
     else if (k == "frontier_threads") g.opt.frontier_threads = std::max<int64_t>(32, std::min<int64_t>(512, value));
     else if (k == "warp_max_n") g.opt.warp_max_n = std::max<int64_t>(0, value);
-    else if (k == "iter_mult") g.opt.iter_mult = std::max<int64_t>(1, std::min<int64_t>(1 << 20, value));
+    else if (k == "iter_mult") g.opt.iter_mult = std::max<int64_t>(0, std::min<int64_t>(1 << 20, value));
     else if (k == "ws_budget_mb") g.opt.ws_budget_mb = std::max<int64_t>(0, value);
     else if (k == "order_min_n") g.opt.order_min_n = std::max<int64_t>(0, value);
     else if (k == "csr_device_min_m") g.opt.csr_device_min_m = std::max<int64_t>(0, value);

@@ -81,7 +81,9 @@ const char* fbc_last_error_string(void);
  * "block_threads", "frontier_threads", "group" (sources per block of the frontier kernel:
  * 1, 2, 4, or 0 = automatic), "chunk_max", "wide_n", "warp_max_n" (largest segment run
  * warp-per-source), "order_min_n" (batched runs relabel graphs of at least this many vertices
- * for memory locality, outputs in input ids), "iter_mult", "ws_budget_mb".
+ * for memory locality, outputs in input ids), "iter_mult" (distance-pass rounds are capped at
+ * iter_mult * (n + 2); 0 makes every unit stop at once with FBC_ERR_ITER_LIMIT, a host-side way to
+ * exercise the bounded-loop error path), "ws_budget_mb".
  * Unknown key -> FBC_ERR_INVALID_ARG. */
 int fbc_set_option(const char* key, int64_t value);
 int fbc_get_option(const char* key, int64_t* value);
