@@ -185,6 +185,14 @@ class Workload:
     def cpu_sample(self, threads, budget_s):
         raise NotImplementedError
 
+    def tune(self, fg, prec):
+        """Autotune the batched schedule's knobs for this workload; returns the choice."""
+        return {}
+
+    def knobs(self, fg, phase):
+        for k, v in getattr(self, "tuned", {}).get(phase, {}).items():
+            fg.set_option(k, v)
+
 
 def _pivots_for(off, cv, frac, seed):
     """Synthetic pivot classes: about `frac` of each cluster's vertices, cardinalities summing to
@@ -261,10 +269,21 @@ class GridClustered4M(Workload):
 
     def step(self, fg, prec, sched):
         st1, st2 = fg.Stats(), fg.Stats()
+        self.knobs(fg, "clusters")
         ev = fg.cluster_eval_batch(self.g, self.cs, prec, sched, stats=st1)
+        self.knobs(fg, "pivots")
         self.last = fg.dependency_batch(self.g, self.pv, self.kv, prec, sched, out=ev.intra_bc.copy(),
                                         stats=st2)
         return [st1, st2]
+
+    def tune(self, fg, prec):
+        import autotune
+
+        self.tuned = {"clusters": autotune.tune_clusters(self.g, self.cs, prec, sample=4, deltas=(2, 4),
+                                                        chunks=(512,), threads=(64, 128)),
+                      "pivots": autotune.tune_pivots(self.g, self.pv, self.kv, prec, sample=304,
+                                                     deltas=(2, 4, 8), threads=(128,))}
+        return self.tuned
 
     def cpu_sample(self, threads, budget_s):
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -296,8 +315,16 @@ class ExactWorkload(Workload):
 
     def step(self, fg, prec, sched):
         st = fg.Stats()
+        self.knobs(fg, "exact")
         self.last = fg.exact_bc(self.g, prec, sched, stats=st)
         return [st]
+
+    def tune(self, fg, prec):
+        import autotune
+
+        src = np.arange(self.el.n, dtype=np.int32)
+        self.tuned = {"exact": autotune.tune_pivots(self.g, src, None, prec, sample=min(4096, self.el.n))}
+        return self.tuned
 
     def cpu_sample(self, threads, budget_s):
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -330,6 +357,7 @@ class MultiGraph(Workload):
                        "relaxations_per_step": self.work}
 
     def step(self, fg, prec, sched):
+        self.knobs(fg, "graphs")
         if self.sequential:
             out = []
             for g in self.gs:
@@ -340,6 +368,15 @@ class MultiGraph(Workload):
         st = fg.Stats()
         fg.multi_exact_bc(self.gs, prec, sched, stats=st)
         return [st]
+
+    def tune(self, fg, prec):
+        """On the largest graph (most of the work): a sample of its sources."""
+        import autotune
+
+        i = int(np.argmax([e.n for e in self.els]))
+        src = np.arange(self.els[i].n, dtype=np.int32)
+        self.tuned = {"graphs": autotune.tune_pivots(self.gs[i], src, None, prec, sample=2048)}
+        return self.tuned
 
     def cpu_sample(self, threads, budget_s):
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -382,6 +419,7 @@ def run_extra(args):
     sched = fg.BATCHED if args.sched == "batched" else fg.PLAIN
     wl = EXTRA_WORKLOADS[args.workload]()
     wl.setup(fg, args)
+    tuned = wl.tune(fg, prec) if sched == fg.BATCHED and not args.no_autotune else {}
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     for _ in range(args.warmup):
         wl.step(fg, prec, sched)
@@ -408,7 +446,7 @@ def run_extra(args):
     line = {"metric": METRIC, "value": wl.work * args.steps / dev / 1e9, "unit": "GTEPS", "n_gpus": 1,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev / args.steps * 1e3,
             "higher_is_better": True, "dtype": "f32x2+u64" if prec == fg.FP32C else "f64+u64",
-            "config": dict(wl.config, precision=args.prec, schedule=args.sched),
+            "config": dict(wl.config, precision=args.prec, schedule=args.sched, autotuned=tuned),
             "e2e": {"value": wl.work * args.steps / wall / 1e9, "unit": "GTEPS"},
             "gpu_launches": launches,
             "roofline": {"kernel": dom, "achieved": achieved, "unit": "GB/s"}}

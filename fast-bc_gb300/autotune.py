@@ -60,9 +60,10 @@ def tune_pivots(g: fg.Graph, sources, cards=None, precision: int = fg.FP32C, sam
 
 
 def tune_clusters(g: fg.Graph, cs: fg.ClusterSet, precision: int = fg.FP32C, sample: int = 16,
-                  deltas=(2, 4, 8), chunks=(128, 512)) -> dict:
-    """Cluster sources: delta and the shared-memory kernel's chunk size, on a sample of the
-    clusters (every k-th, keeping the size mix)."""
+                  deltas=(2, 4, 8), chunks=(128, 512), threads=(128,)) -> dict:
+    """Cluster sources: delta, the shared-memory kernel's chunk size and (for clusters too large
+    for shared memory) the frontier kernel's block size, on a sample of the clusters (every k-th,
+    keeping the size mix)."""
     cs = cs.with_borders(g)
     k = max(1, cs.count // sample)
     pick = list(range(0, cs.count, k))
@@ -70,8 +71,8 @@ def tune_clusters(g: fg.Graph, cs: fg.ClusterSet, precision: int = fg.FP32C, sam
                                    [cs.borders[cs.boff[c]:cs.boff[c + 1]] for c in pick])
     mw = _mean_weight(g)
     best, arg = float("inf"), None
-    for dm, ch in itertools.product(deltas, chunks):
-        choice = {"delta": max(1, int(round(dm * mw))), "chunk_max": ch}
+    for dm, ch, bt in itertools.product(deltas, chunks, threads):
+        choice = {"delta": max(1, int(round(dm * mw))), "chunk_max": ch, "frontier_threads": bt}
         _apply(choice)
         t = _time(lambda st: fg.cluster_eval_batch(g, sub, precision, fg.BATCHED, stats=st))
         if t < best:
