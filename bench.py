@@ -576,10 +576,23 @@ def main():
     borders = [bv[boff[c]:boff[c + 1]] for c in keep]
     pivots = [pv[poff[c]:poff[c + 1]] for c in range(off.size - 1)]
     cards = [kv[poff[c]:poff[c + 1]] for c in range(off.size - 1)]
-    cs = fg.ClusterSet.from_lists(clusters, borders)
     g = fg.Graph.from_edgelist(el)  # resident for the whole run
-    allp = np.concatenate(pivots).astype(np.int32)
-    allc = np.concatenate(cards).astype(np.float64)
+    # the step's inputs and outputs live in page-locked host memory (copied every step)
+    pinned_keep = []
+
+    def pinned(a):
+        a = np.ascontiguousarray(a)
+        wide = a.dtype == np.uint64
+        t = torch.empty(a.size, dtype=torch.from_numpy(a.view(np.int64) if wide else a).dtype, pin_memory=True)
+        pinned_keep.append(t)
+        out = t.numpy().view(np.uint64) if wide else t.numpy()
+        out[:] = a
+        return out
+
+    cs0 = fg.ClusterSet.from_lists(clusters, borders)
+    cs = fg.ClusterSet(pinned(cs0.off), pinned(cs0.vertices), pinned(cs0.boff), pinned(cs0.borders))
+    allp = pinned(np.concatenate(pivots).astype(np.int32))
+    allc = pinned(np.concatenate(cards).astype(np.float64))
     work = work_per_step(el, z, keep)
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
 
@@ -594,17 +607,21 @@ def main():
         for k, v in tuned.get(phase, {}).items():
             fg.set_option(k, v)
 
-    prev = {}
+    # output arrays, reused from step to step as a caller running the sweep repeatedly would
+    entry_off = np.zeros(cs.count + 1, np.int64)
+    entry_off[1:] = np.cumsum(np.diff(cs.off) * np.diff(cs.boff))
+    ent = int(entry_off[-1])
+    prev = {"ev": fg.ClusterEval(pinned(np.zeros(g.n)), pinned(np.zeros(ent)), pinned(np.zeros(ent, np.uint64)),
+                                 cs, entry_off)}
+    bcbuf = pinned(np.zeros(g.n))
 
     def step():
         st1, st2 = fg.Stats(), fg.Stats()
         knobs("clusters")
-        # the caller's output arrays are reused from step to step, as a caller running the
-        # sweep repeatedly would (fresh arrays would add page faults to every download)
-        ev = fg.cluster_eval_batch(g, cs, prec, sched, stats=st1, out=prev.get("ev"))
-        prev["ev"] = ev
+        ev = fg.cluster_eval_batch(g, cs, prec, sched, stats=st1, out=prev["ev"])
         knobs("pivots")
-        bc = fg.dependency_batch(g, allp, allc, prec, sched, out=ev.intra_bc.copy(), stats=st2)
+        bcbuf[:] = ev.intra_bc
+        bc = fg.dependency_batch(g, allp, allc, prec, sched, out=bcbuf, stats=st2)
         for c in range(len(clusters)):
             tot = float(np.sum(cards[keep[c]]))
             if tot:
