@@ -660,7 +660,7 @@ int run_plan_t(Plan& P, fbc_stats* st) {
     std::stable_sort(ub.begin(), ub.end(), [&](const Unit& a, const Unit& b) {
         return P.segs[a.seg].n > P.segs[b.seg].n;
     });
-    // the batched block kernel keeps tight in-edge counts in 16 bits
+    // the batched block kernel keeps tight in-edge counts in at most 16 bits
     if (P.sched == FBC_SCHED_BATCHED)
         for (const Unit& u : ub)
             if (P.seg_maxindeg[u.seg] >= 65535) {

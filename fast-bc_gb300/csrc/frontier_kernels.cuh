@@ -61,7 +61,7 @@ __host__ __device__ inline int64_t fqcap(int64_t cap) {
 
 // Path count and dependency of a vertex side by side, so the dependency pass reads both with
 // one 16-byte load.  Until the dependency pass writes it, the dependency slot holds the
-// vertex's tight out-edge mask (bit k: edge e0 + k; all ones for rows longer than 32 edges),
+// vertex's tight out-edge mask (bit k: edge e0 + k; all ones for rows of B or more edges),
 // so the Kahn pass finds a released vertex's mask in the sector its count atomic just touched.
 template <class Prec>
 struct __align__(16) FRec {
