@@ -92,7 +92,6 @@ struct Options {
     int64_t order_min_n = 131072;  // batched runs relabel graphs of at least this many vertices
     int64_t csr_device_min_m = 65536;  // edge lists of at least this many edges are built on the device
     int64_t wide_threads = 512;        // block size of the wide frontier kernel (<= 512)
-    int64_t warp_smem = 1;      // batched: warp state in shared memory when it fits
     int64_t debug_sched = FBC_SCHED_PLAIN;  // schedule used by fbc_sssp_debug
 };
 
@@ -1191,7 +1190,6 @@ int fbc_set_option(const char* key, int64_t value) {
         if (value != 0 && value != 1 && value != 2 && value != 4) return fail(FBC_ERR_INVALID_ARG, "group must be 0, 1, 2 or 4");
         g.opt.group = value;
     }
-    else if (k == "warp_smem") g.opt.warp_smem = value ? 1 : 0;
     else if (k == "debug_sched") g.opt.debug_sched = value ? FBC_SCHED_BATCHED : FBC_SCHED_PLAIN;
     else return fail(FBC_ERR_INVALID_ARG, "unknown option " + k);
     return FBC_OK;
@@ -1213,7 +1211,6 @@ int fbc_get_option(const char* key, int64_t* value) {
     else if (k == "order_min_n") *value = g.opt.order_min_n;
     else if (k == "csr_device_min_m") *value = g.opt.csr_device_min_m;
     else if (k == "wide_threads") *value = g.opt.wide_threads;
-    else if (k == "warp_smem") *value = g.opt.warp_smem;
     else if (k == "debug_sched") *value = g.opt.debug_sched;
     else return fail(FBC_ERR_INVALID_ARG, "unknown option " + k);
     return FBC_OK;
