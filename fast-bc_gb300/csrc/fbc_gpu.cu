@@ -15,6 +15,7 @@
 #include <vector>
 
 #include "cluster_build.cuh"
+#include "classes.cuh"
 #include "graph_build.cuh"
 #include "frontier_kernels.cuh"
 
@@ -1425,6 +1426,141 @@ int fbc_cluster_borders(fbc_graph G, int32_t nclusters, const int64_t* coff, con
     FBC_TRY(device_borders(G, nclusters, coff, boff, bl, nullptr));
     if (out_boff) std::copy(boff.begin(), boff.end(), out_boff);
     if (out_borders) std::copy(bl.begin(), bl.end(), out_borders);
+    return FBC_OK;
+}
+
+int fbc_cluster_classes(fbc_graph G, int32_t nclusters, const int64_t* coff, const int32_t* cverts,
+                        const int64_t* border_off, const int32_t* borders, const double* bc,
+                        const double* bdist, const uint64_t* bsig, int64_t* out_class_off,
+                        int32_t* out_pivots, int32_t* out_cards) {
+    std::lock_guard<std::recursive_mutex> lk(g_mu);
+    FBC_TRY(check_init());
+    if (!G || !bc || !out_class_off || (border_off && !borders)) return fail(FBC_ERR_INVALID_ARG, "null argument");
+    FBC_TRY(device_cluster_ids(G, nclusters, coff, cverts, nullptr));
+    const int64_t nv = coff[nclusters];
+    std::vector<int64_t> boff_v;
+    std::vector<int32_t> bl_v;
+    if (!border_off) {
+        FBC_TRY(device_borders(G, nclusters, coff, boff_v, bl_v, nullptr));
+        border_off = boff_v.data();
+    } else {
+        if (border_off[0] != 0) return fail(FBC_ERR_INVALID_ARG, "border_off[0] must be 0");
+        for (int32_t c = 0; c < nclusters; ++c)
+            if (border_off[c + 1] < border_off[c]) return fail(FBC_ERR_INVALID_ARG, "border_off is not monotone");
+        const int64_t nb = border_off[nclusters];
+        FBC_CK(g.c_bsrc.ensure(sizeof(int32_t) * (size_t)std::max<int64_t>(nb, 1)));
+        FBC_CK(g.c_boff.ensure(sizeof(int64_t) * ((size_t)nclusters + 1)));
+        if (nb > 0)
+            FBC_CK(cudaMemcpyAsync(g.c_bsrc.p, borders, sizeof(int32_t) * (size_t)nb, cudaMemcpyHostToDevice, g.st));
+        FBC_CK(cudaMemcpyAsync(g.c_boff.p, border_off, sizeof(int64_t) * ((size_t)nclusters + 1),
+                               cudaMemcpyHostToDevice, g.st));
+    }
+    const int64_t nbt = border_off[nclusters];
+    if (nv > 0 && (!out_pivots || !out_cards)) return fail(FBC_ERR_INVALID_ARG, "null argument");
+    // border-vector entries and table slots of every cluster
+    std::vector<int64_t> eoff((size_t)nclusters + 1, 0), toff((size_t)nclusters + 1, 0);
+    for (int32_t c = 0; c < nclusters; ++c) {
+        const int64_t nc = coff[c + 1] - coff[c];
+        eoff[c + 1] = eoff[c] + nc * (border_off[c + 1] - border_off[c]);
+        int64_t t = 2;
+        while (t < 2 * nc) t <<= 1;
+        toff[c + 1] = toff[c] + (nc > 0 ? t : 0);
+    }
+    if ((bdist == nullptr || bsig == nullptr) && eoff[nclusters] > 0) return fail(FBC_ERR_INVALID_ARG, "null argument");
+    TmpBuf d_eoff, d_toff, d_bd, d_bs, d_bc, thash, tfirst, vhash, vrep, flag, scan, isb, cbord, card, minbc, pick, piv, crd;
+    const size_t ne = (size_t)std::max<int64_t>(eoff[nclusters], 1), nts = (size_t)std::max<int64_t>(toff[nclusters], 1);
+    const size_t nvv = (size_t)std::max<int64_t>(nv, 1);
+    FBC_CK(d_eoff.ensure(sizeof(int64_t) * eoff.size()));
+    FBC_CK(d_toff.ensure(sizeof(int64_t) * toff.size()));
+    FBC_CK(d_bd.ensure(sizeof(double) * ne));
+    FBC_CK(d_bs.ensure(sizeof(uint64_t) * ne));
+    FBC_CK(d_bc.ensure(sizeof(double) * (size_t)std::max(G->n, 1)));
+    FBC_CK(thash.ensure(sizeof(unsigned long long) * nts));
+    FBC_CK(tfirst.ensure(sizeof(int) * nts));
+    FBC_CK(vhash.ensure(sizeof(unsigned long long) * nvv));
+    FBC_CK(vrep.ensure(sizeof(int) * nvv));
+    FBC_CK(flag.ensure(sizeof(int32_t) * nvv));
+    FBC_CK(scan.ensure(sizeof(int32_t) * (nvv + 1)));
+    FBC_CK(isb.ensure(nvv));
+    FBC_CK(cbord.ensure(sizeof(int32_t) * (size_t)std::max<int64_t>(nbt, 1)));
+    FBC_CK(cudaMemcpyAsync(d_eoff.p, eoff.data(), sizeof(int64_t) * eoff.size(), cudaMemcpyHostToDevice, g.st));
+    FBC_CK(cudaMemcpyAsync(d_toff.p, toff.data(), sizeof(int64_t) * toff.size(), cudaMemcpyHostToDevice, g.st));
+    if (eoff[nclusters] > 0) {
+        FBC_CK(cudaMemcpyAsync(d_bd.p, bdist, sizeof(double) * (size_t)eoff[nclusters], cudaMemcpyHostToDevice, g.st));
+        FBC_CK(cudaMemcpyAsync(d_bs.p, bsig, sizeof(uint64_t) * (size_t)eoff[nclusters], cudaMemcpyHostToDevice, g.st));
+    }
+    FBC_CK(cudaMemcpyAsync(d_bc.p, bc, sizeof(double) * (size_t)G->n, cudaMemcpyHostToDevice, g.st));
+    FBC_CK(cudaMemsetAsync(thash.p, 0, sizeof(unsigned long long) * nts, g.st));
+    FBC_CK(cudaMemsetAsync(tfirst.p, 0x7f, sizeof(int) * nts, g.st));
+    FBC_CK(cudaMemsetAsync(isb.p, 0, nvv, g.st));
+    g_aux_launches = 0;
+    if (nbt > 0) {
+        fbc::clu_border_map_kernel<<<grid_for(nbt), 256, 0, g.st>>>(nbt, g.c_boff.as<int64_t>(), nclusters,
+                                                                    g.c_bsrc.as<int32_t>(), G->n, g.c_id.as<int32_t>(),
+                                                                    g.c_lid.as<int32_t>(), cbord.as<int32_t>(),
+                                                                    g.c_err.as<int>());
+        fbc::cls_mark_border_kernel<<<grid_for(nbt), 256, 0, g.st>>>(nbt, g.c_boff.as<int64_t>(), nclusters,
+                                                                     g.c_off.as<int64_t>(), cbord.as<int32_t>(),
+                                                                     isb.as<uint8_t>());
+    }
+    FBC_CK(cudaGetLastError());
+    int err = 0;
+    FBC_CK(cudaMemcpyAsync(&err, g.c_err.p, sizeof(int), cudaMemcpyDeviceToHost, g.st));
+    FBC_CK(cudaStreamSynchronize(g.st));
+    FBC_TRY(cluster_error(err));
+    FBC_CK(cudaMemsetAsync(g.c_err.p, 0, sizeof(int), g.st));  // the class kernels' own bits
+    fbc::ClsArgs A{};
+    A.coff = g.c_off.as<int64_t>();
+    A.boff = g.c_boff.as<int64_t>();
+    A.eoff = d_eoff.as<int64_t>();
+    A.toff = d_toff.as<int64_t>();
+    A.ncl = nclusters;
+    A.nv = nv;
+    A.bdist = d_bd.as<double>();
+    A.bsig = d_bs.as<unsigned long long>();
+    A.thash = thash.as<unsigned long long>();
+    A.tfirst = tfirst.as<int>();
+    A.vhash = vhash.as<unsigned long long>();
+    A.vrep = vrep.as<int>();
+    A.err = g.c_err.as<int>();
+    if (nv > 0) {
+        fbc::cls_hash_kernel<<<grid_for(nv), 256, 0, g.st>>>(A);
+        fbc::cls_rep_kernel<<<grid_for(nv), 256, 0, g.st>>>(A);
+        fbc::cls_flag_kernel<<<grid_for(nv), 256, 0, g.st>>>(A, flag.as<int32_t>());
+        FBC_CK(cudaGetLastError());
+    }
+    FBC_TRY(device_scan(flag.as<int32_t>(), nv, scan.as<int32_t>()));
+    std::vector<int32_t> sc((size_t)nv + 1);
+    FBC_CK(cudaMemcpyAsync(sc.data(), scan.p, sizeof(int32_t) * sc.size(), cudaMemcpyDeviceToHost, g.st));
+    FBC_CK(cudaMemcpyAsync(&err, g.c_err.p, sizeof(int), cudaMemcpyDeviceToHost, g.st));
+    FBC_CK(cudaStreamSynchronize(g.st));
+    if (err & fbc::kClsCollision) return fail(FBC_ERR_HASH, "two different border vectors share a hash");
+    if (err & fbc::kClsFull) return fail(FBC_ERR_QUEUE, "class table full (sizing)");
+    const int32_t ncls = sc[(size_t)nv];
+    for (int32_t c = 0; c <= nclusters; ++c) out_class_off[c] = sc[(size_t)coff[c]];
+    if (ncls > 0) {
+        FBC_CK(card.ensure(sizeof(int) * (size_t)ncls));
+        FBC_CK(minbc.ensure(sizeof(unsigned long long) * (size_t)ncls));
+        FBC_CK(pick.ensure(sizeof(int) * (size_t)ncls));
+        FBC_CK(piv.ensure(sizeof(int32_t) * (size_t)ncls));
+        FBC_CK(crd.ensure(sizeof(int32_t) * (size_t)ncls));
+        FBC_CK(cudaMemsetAsync(card.p, 0, sizeof(int) * (size_t)ncls, g.st));
+        FBC_CK(cudaMemsetAsync(minbc.p, 0xff, sizeof(unsigned long long) * (size_t)ncls, g.st));
+        FBC_CK(cudaMemsetAsync(pick.p, 0x7f, sizeof(int) * (size_t)ncls, g.st));
+        fbc::cls_card_kernel<<<grid_for(nv), 256, 0, g.st>>>(A, scan.as<int32_t>(), g.cgid.as<int32_t>(),
+                                                             isb.as<uint8_t>(), d_bc.as<double>(), card.as<int>(),
+                                                             minbc.as<unsigned long long>());
+        fbc::cls_pick_kernel<<<grid_for(nv), 256, 0, g.st>>>(A, scan.as<int32_t>(), g.cgid.as<int32_t>(),
+                                                             isb.as<uint8_t>(), d_bc.as<double>(),
+                                                             minbc.as<unsigned long long>(), pick.as<int>());
+        fbc::cls_out_kernel<<<grid_for(nv), 256, 0, g.st>>>(A, flag.as<int32_t>(), scan.as<int32_t>(),
+                                                            g.cgid.as<int32_t>(), card.as<int>(), pick.as<int>(),
+                                                            piv.as<int32_t>(), crd.as<int32_t>());
+        FBC_CK(cudaGetLastError());
+        FBC_CK(cudaMemcpyAsync(out_pivots, piv.p, sizeof(int32_t) * (size_t)ncls, cudaMemcpyDeviceToHost, g.st));
+        FBC_CK(cudaMemcpyAsync(out_cards, crd.p, sizeof(int32_t) * (size_t)ncls, cudaMemcpyDeviceToHost, g.st));
+        FBC_CK(cudaStreamSynchronize(g.st));
+    }
     return FBC_OK;
 }
 

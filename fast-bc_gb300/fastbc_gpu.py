@@ -35,6 +35,7 @@ FBC_ERR_RANGE = 5
 FBC_ERR_SIGMA_OVERFLOW = 6
 FBC_ERR_NOT_INIT = 7
 FBC_ERR_QUEUE = 8
+FBC_ERR_HASH = 9
 
 FP64 = 0
 FP32C = 1
@@ -86,6 +87,7 @@ def _load():
                                     P(Stats)], C.c_int),
         "fbc_multi_exact_bc": ([i32, vp, C.c_int, C.c_int, vp, P(Stats)], C.c_int),
         "fbc_sssp_debug": ([vp, i32, vp, vp, vp, vp], C.c_int),
+        "fbc_cluster_classes": ([vp, i32, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp], C.c_int),
         "fbc_cluster_plan_create": ([vp, i32, vp, vp, vp, vp, C.c_int, P(vp)], C.c_int),
         "fbc_plan_run": ([vp, P(Stats)], C.c_int),
         "fbc_plan_results": ([vp, P(vp), P(vp), P(vp), P(i64), P(i32)], C.c_int),
@@ -360,6 +362,24 @@ class ClusterPlan:
             self.free()
         except Exception:
             pass
+
+
+def cluster_classes(g: Graph, cs: ClusterSet, bc, ev: ClusterEval):
+    """VertexInfoPivotSelector::selectPivots for every cluster (exact topological classes):
+    per cluster, (pivots, cardinalities) in class order.  `bc` is the BC the selection compares
+    (the intra-cluster BC), `ev` the border vectors of a cluster_eval_batch on the same clusters."""
+    cs = cs.with_borders(g)
+    bcv = np.ascontiguousarray(bc, np.float64)
+    coff = np.zeros(cs.count + 1, np.int64)
+    piv = np.zeros(max(int(cs.off[-1]), 1), np.int32)
+    crd = np.zeros(max(int(cs.off[-1]), 1), np.int32)
+    bl = cs.borders if cs.borders.size else np.zeros(1, np.int32)
+    bd = ev.border_dist if ev.border_dist.size else np.zeros(1)
+    bs = ev.border_sigma if ev.border_sigma.size else np.zeros(1, np.uint64)
+    _ck(lib.fbc_cluster_classes(g._h, cs.count, _ptr(cs.off), _ptr(cs.vertices), _ptr(cs.boff), _ptr(bl),
+                                _ptr(bcv), _ptr(np.ascontiguousarray(bd)), _ptr(np.ascontiguousarray(bs)),
+                                _ptr(coff), _ptr(piv), _ptr(crd)))
+    return [(piv[coff[c]:coff[c + 1]].copy(), crd[coff[c]:coff[c + 1]].copy()) for c in range(cs.count)]
 
 
 def multi_exact_bc(graphs: list[Graph], precision: int = FP64, sched: int = BATCHED,

@@ -37,6 +37,8 @@ extern "C" {
 #define FBC_ERR_SIGMA_OVERFLOW 6 /* a shortest-path count exceeded 2^64-1                */
 #define FBC_ERR_NOT_INIT 7      /* fbc_gpu_init has not been called                     */
 #define FBC_ERR_QUEUE 8         /* a device work queue overflowed (internal error)      */
+#define FBC_ERR_HASH 9          /* two different border vectors share one 64-bit hash in the
+                                   class grouping (reported, never merged)               */
 
 /* dependency precision (the "precision" form of the engine) */
 #define FBC_PREC_FP64 0   /* plain: FP64 dependency arithmetic                          */
@@ -159,6 +161,20 @@ int fbc_plan_run(fbc_plan p, fbc_stats* st);
 int fbc_plan_results(fbc_plan p, const double** intra_bc, const double** border_dist,
                      const uint64_t** border_sigma, int64_t* entries, int32_t* captured);
 int fbc_plan_free(fbc_plan p);
+
+/* Topological classes of every cluster (VertexInfoPivotSelector::selectPivots,
+ * VertexInfoPivotSelector.h:30-123, for all clusters): vertices of a cluster whose border vectors
+ * (bdist / bsig as fbc_cluster_eval_batch lays them out), lengths shifted by their minimum, are
+ * equal form a class; classes in the order of their first member in the cluster list; a class's
+ * pivot is its non-border member of least bc[v] (first in list order on ties), or its first member
+ * if all members are borders; cardinality = class size.  Clusters without borders get no class.
+ * Outputs: out_class_off[nclusters + 1] (classes of cluster c at [off[c], off[c+1])), out_pivots
+ * and out_cards with room for cluster_off[nclusters] entries.  bc has n entries (the intra-cluster
+ * BC the selection compares). */
+int fbc_cluster_classes(fbc_graph g, int32_t nclusters, const int64_t* cluster_off,
+                        const int32_t* cluster_vertices, const int64_t* border_off, const int32_t* borders,
+                        const double* bc, const double* border_dist, const uint64_t* border_sigma,
+                        int64_t* out_class_off, int32_t* out_pivots, int32_t* out_cards);
 
 /* Exact BC of several independent graphs in one persistent launch.  out_bc[g] has
  * n_g entries. */

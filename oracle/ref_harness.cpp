@@ -12,6 +12,9 @@
 //             dumping the partition, borders, pivots and cardinalities, the intra-cluster
 //             BC and the final BC, and also runs computeBC itself to cross-check the replay.
 //   partition <edges> <seeds> <prec> <out>          LouvainGraphPartition alone: the communities
+//   classes   <edges> <clusters> <out_prefix>       cluster evaluation + VertexInfoPivotSelector per
+//                                                   cluster (clusters file: one line per cluster,
+//                                                   "count v1 v2 ..."): exact classes' pivots/sizes
 //   pins                                            the reference unit-test scenarios on DWGtext
 #define FASTBC_BRANDES_ENABLE_PIVOT_BORDER
 #define FASTBC_BRANDES_CLUSTERED_IGNORE_UNCONNECTED
@@ -60,6 +63,19 @@ static std::vector<V> read_ints(const char* path) {
     std::vector<V> out;
     V x;
     while (f >> x) out.push_back(x);
+    return out;
+}
+
+// one cluster per line: "count v1 v2 ..."
+static std::vector<std::vector<V>> read_clusters(const char* path) {
+    std::ifstream f(path);
+    std::vector<std::vector<V>> out;
+    size_t k;
+    while (f >> k) {
+        std::vector<V> c(k);
+        for (auto& v : c) f >> v;
+        out.push_back(std::move(c));
+    }
     return out;
 }
 
@@ -118,6 +134,37 @@ int main(int argc, char** argv) {
         for (const auto& c : comms) {
             std::fprintf(f, "%zu", c.size());
             for (V v : c) std::fprintf(f, " %d", v);
+            std::fprintf(f, "\n");
+        }
+        std::fclose(f);
+        return 0;
+    }
+    if (mode == "classes" && argc == 5) {
+        // VertexInfoPivotSelector::selectPivots (VertexInfoPivotSelector.h:30-123) on every
+        // cluster of a given partition, after DijkstraClusterEvaluator::evaluateCluster: the exact
+        // topological classes' pivots and cardinalities, per cluster, plus the intra-cluster BC.
+        auto g = load(argv[2]);
+        auto clusters = read_clusters(argv[3]);
+        std::string pre = argv[4];
+        const size_t n = g->vertices().size();
+        std::vector<W> bc(n, 0.0);
+        std::vector<std::shared_ptr<fastbc::brandes::VertexInfo<V, W>>> vi(n, nullptr);
+        fastbc::brandes::DijkstraClusterEvaluator<V, W> ce;
+        fastbc::brandes::VertexInfoPivotSelector<V, W> ps;
+        std::vector<std::shared_ptr<fastbc::SubGraph<V, W>>> sgs;
+        for (auto& c : clusters) {
+            sgs.push_back(std::make_shared<fastbc::SubGraph<V, W>>(c, g));
+            if (!sgs.back()->borders().empty()) ce.evaluateCluster(bc, vi, sgs.back());
+        }
+        dump_vec((pre + ".intra").c_str(), bc);
+        FILE* f = std::fopen((pre + ".classes").c_str(), "w");
+        for (auto& sg : sgs) {
+            if (sg->borders().empty()) { std::fprintf(f, "0\n0\n"); continue; }
+            auto piv = ps.selectPivots(bc, vi, sg->vertices(), sg->borders());
+            std::fprintf(f, "%zu", piv.first.size());
+            for (V v : piv.first) std::fprintf(f, " %d", v);
+            std::fprintf(f, "\n%zu", piv.second.size());
+            for (V k : piv.second) std::fprintf(f, " %d", k);
             std::fprintf(f, "\n");
         }
         std::fclose(f);

@@ -8,6 +8,9 @@ oracle/_ref/ref_harness) single-threaded on the seeded workloads and stores:
                              precision 0.01, kfrac 0.5): partition, borders, pivots and
                              cardinalities, intra-cluster BC, final BC (step replay and the
                              reference's own ClusteredBrandeBC::computeBC)
+  grid256_classes.npz        VertexInfoPivotSelector (the exact topological classes) on every
+                             cluster of that partition after DijkstraClusterEvaluator: class
+                             offsets, pivots, cardinalities, and the intra-cluster BC it compared
   grid2048_partition.npz     LouvainGraphPartition (seeds 1-4, precision 0.01) of the
                              2048x2048 grid: community id per vertex (int16; every
                              community's vertices are ascending, as the reference lists them)
@@ -93,6 +96,28 @@ def main():
                         cluster_vertices=cv, border_off=boff, borders=bv, pivot_off=poff,
                         pivots=pv, cards=kv, intra_bc=np.loadtxt(pre + ".intra"), bc=bc_ref,
                         bc_replay=bc)
+    clu = os.path.join(work, "grid256.clu")
+    with open(clu, "w") as f:
+        for c in range(coff.size - 1):
+            vs = cv[coff[c]:coff[c + 1]]
+            f.write(f"{vs.size} " + " ".join(map(str, vs)) + "\n")
+    cls = os.path.join(work, "grid256cls")
+    subprocess.run([HARNESS, "classes", g256, clu, cls], check=True, env=dict(os.environ, OMP_NUM_THREADS="8"))
+    with open(cls + ".classes") as f:
+        lines = f.read().split("\n")
+    piv, crd = [], []
+    for c in range(coff.size - 1):
+        a = list(map(int, lines[2 * c].split()))
+        b = list(map(int, lines[2 * c + 1].split()))
+        assert a[0] == len(a) - 1 == b[0] == len(b) - 1
+        piv.append(np.array(a[1:], np.int32))
+        crd.append(np.array(b[1:], np.int32))
+    class_off = np.zeros(len(piv) + 1, np.int64)
+    class_off[1:] = np.cumsum([p.size for p in piv])
+    # the BC the selector compared is stored with it (OpenMP reductions round differently)
+    np.savez_compressed(os.path.join(HERE, "grid256_classes.npz"), class_off=class_off,
+                        pivots=np.concatenate(piv), cards=np.concatenate(crd),
+                        intra_bc=np.loadtxt(cls + ".intra"))
     g2048 = os.path.join(work, "grid2048.txt")
     if not os.path.exists(g2048):
         graphs.WORKLOADS["grid2048"]().write(g2048)
