@@ -165,6 +165,18 @@ struct fbc_plan_s {
     int64_t nunits = 0;
     std::vector<int64_t> coff, boff;
     std::vector<int32_t> cverts, borders;
+    // frees everything the plan holds, also when its creation stopped half way
+    ~fbc_plan_s() {
+        if (g.init) cudaStreamSynchronize(g.st);  // no launch in flight still uses a buffer
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        for (DBuf* b : {&crp, &cadj, &cgid, &cbord, &segs, &units, &chunks, &bc, &bdist, &bsig, &ctr, &retry})
+            b->release();
+        if (h_bc) cudaFreeHost(h_bc);
+        if (h_bdist) cudaFreeHost(h_bdist);
+        if (h_bsig) cudaFreeHost(h_bsig);
+        if (h_ctl) cudaFreeHost(h_ctl);
+    }
 };
 
 namespace {
@@ -1742,16 +1754,6 @@ int fbc_plan_results(fbc_plan p, const double** intra_bc, const double** border_
 int fbc_plan_free(fbc_plan p) {
     std::lock_guard<std::recursive_mutex> lk(g_mu);
     if (!p) return FBC_OK;
-    if (g.init) cudaStreamSynchronize(g.st);
-    if (p->exec) cudaGraphExecDestroy(p->exec);
-    if (p->graph) cudaGraphDestroy(p->graph);
-    for (DBuf* b : {&p->crp, &p->cadj, &p->cgid, &p->cbord, &p->segs, &p->units, &p->chunks, &p->bc,
-                    &p->bdist, &p->bsig, &p->ctr, &p->retry})
-        b->release();
-    if (p->h_bc) cudaFreeHost(p->h_bc);
-    if (p->h_bdist) cudaFreeHost(p->h_bdist);
-    if (p->h_bsig) cudaFreeHost(p->h_bsig);
-    if (p->h_ctl) cudaFreeHost(p->h_ctl);
     delete p;
     return FBC_OK;
 }

@@ -81,3 +81,34 @@ def test_bad_cluster_lists_rejected(fg):
     # the library stays usable
     ev = fg.cluster_eval_batch(g, fg.ClusterSet.from_lists(good), fg.FP64, fg.BATCHED)
     assert np.all(np.isfinite(ev.intra_bc))
+
+
+def test_failed_plan_create_frees_its_buffers(fg):
+    """A cluster plan whose creation is rejected half way (a border that is not one, found by the
+    device border map after the plan's subgraph buffers exist) leaves no device memory behind,
+    and a valid plan afterwards gives the batched sweep's values."""
+    torch = pytest.importorskip("torch")
+    el = graphs.road_grid(512, 512, seed=4)
+    g = fg.Graph.from_edgelist(el)
+    good = _tiles(el, 512, 128)
+    wrong = fg.ClusterSet.from_lists(good[:2], [good[1][:3], good[0][:3]])
+    with pytest.raises(fg.FbcError):
+        fg.ClusterPlan(g, wrong, fg.FP64)  # first call: the library's own workspaces grow
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    for _ in range(20):
+        with pytest.raises(fg.FbcError) as e:
+            fg.ClusterPlan(g, wrong, fg.FP64)
+        assert e.value.code == fg.FBC_ERR_INVALID_ARG
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    # each leaked attempt would hold the 512x512 cluster CSRs (about 9 MB)
+    assert free0 - free1 < 32 << 20
+    cs = fg.ClusterSet.from_lists(good[:4])
+    plan = fg.ClusterPlan(g, cs, fg.FP64)
+    got = plan.run()
+    ref = fg.cluster_eval_batch(g, cs, fg.FP64, fg.BATCHED)
+    plan.free()
+    assert rel_err(got.intra_bc, ref.intra_bc) <= TOL_FP64
+    assert np.array_equal(got.border_dist, ref.border_dist)
+    assert np.array_equal(got.border_sigma, ref.border_sigma)
