@@ -11,12 +11,16 @@
 #include <memory>
 #include <mutex>
 #include <numeric>
+#include <sstream>
 #include <string>
+#include <locale>
+#include <climits>
 #include <vector>
 
 #include "cluster_build.cuh"
 #include "classes.cuh"
 #include "graph_build.cuh"
+#include "text_parse.cuh"
 #include "frontier_kernels.cuh"
 
 namespace {
@@ -1022,26 +1026,19 @@ struct TmpBuf : DBuf {
     ~TmpBuf() { release(); }
 };
 
-// Edge list -> device CSR (graph_build.cuh).  Returns FBC_OK with *out set, FBC_OK with *out
-// null when a row is longer than the device sort handles (the caller then builds on the host),
-// or an error.
-int device_graph_from_edges(int64_t count, const int32_t* src, const int32_t* dst, const double* w,
-                            fbc_graph* out) {
+// Edge list already on the device -> device CSR (graph_build.cuh).  Returns FBC_OK with *out
+// set, FBC_OK with *out null when a row is longer than the device sort handles (the caller then
+// builds on the host), or an error.  The edge arrays are only read.
+int device_csr_build(int64_t count, const int32_t* dsrc, const int32_t* ddst, const double* dw, fbc_graph* out) {
     *out = nullptr;
-    TmpBuf dsrc, ddst, dw, ints, deg, rs, cursor, keys, ndeg, indeg;
-    FBC_CK(dsrc.ensure(sizeof(int32_t) * (size_t)count));
-    FBC_CK(ddst.ensure(sizeof(int32_t) * (size_t)count));
-    FBC_CK(dw.ensure(sizeof(double) * (size_t)count));
+    TmpBuf ints, deg, rs, cursor, keys, ndeg, indeg;
     FBC_CK(ints.ensure(64));
-    FBC_CK(cudaMemcpyAsync(dsrc.p, src, sizeof(int32_t) * (size_t)count, cudaMemcpyHostToDevice, g.st));
-    FBC_CK(cudaMemcpyAsync(ddst.p, dst, sizeof(int32_t) * (size_t)count, cudaMemcpyHostToDevice, g.st));
-    FBC_CK(cudaMemcpyAsync(dw.p, w, sizeof(double) * (size_t)count, cudaMemcpyHostToDevice, g.st));
     // ints: [0] max source, [1] error bits, [2] max weight, [3] max in-degree, [4..5] weight sum
     int hi[6] = {-1, 0, 0, 0, 0, 0};
     FBC_CK(cudaMemcpyAsync(ints.p, hi, sizeof(hi), cudaMemcpyHostToDevice, g.st));
     int* di = ints.as<int>();
-    fbc::gb_check_kernel<<<grid_for(count), 256, 0, g.st>>>(count, dsrc.as<int32_t>(), ddst.as<int32_t>(),
-                                                            dw.as<double>(), di, di + 1);
+    fbc::gb_check_kernel<<<grid_for(count), 256, 0, g.st>>>(count, dsrc, ddst,
+                                                            dw, di, di + 1);
     FBC_CK(cudaGetLastError());
     FBC_CK(cudaMemcpyAsync(hi, ints.p, 2 * sizeof(int), cudaMemcpyDeviceToHost, g.st));
     FBC_CK(cudaStreamSynchronize(g.st));
@@ -1055,11 +1052,11 @@ int device_graph_from_edges(int64_t count, const int32_t* src, const int32_t* ds
     FBC_CK(ndeg.ensure(sizeof(int32_t) * (size_t)n));
     FBC_CK(cudaMemsetAsync(deg.p, 0, sizeof(int32_t) * (size_t)n, g.st));
     FBC_CK(cudaMemsetAsync(cursor.p, 0, sizeof(int32_t) * (size_t)n, g.st));
-    fbc::gb_count_kernel<<<grid_for(count), 256, 0, g.st>>>(count, dsrc.as<int32_t>(), ddst.as<int32_t>(), n,
+    fbc::gb_count_kernel<<<grid_for(count), 256, 0, g.st>>>(count, dsrc, ddst, n,
                                                             deg.as<int32_t>(), di + 1);
     FBC_CK(cudaGetLastError());
     FBC_TRY(device_scan(deg.as<int32_t>(), n, rs.as<int32_t>()));
-    fbc::gb_scatter_kernel<<<grid_for(count), 256, 0, g.st>>>(count, dsrc.as<int32_t>(), ddst.as<int32_t>(),
+    fbc::gb_scatter_kernel<<<grid_for(count), 256, 0, g.st>>>(count, dsrc, ddst,
                                                               rs.as<int32_t>(), cursor.as<int32_t>(),
                                                               keys.as<unsigned long long>());
     fbc::gb_sort_rows_kernel<<<grid_for(n), 256, 0, g.st>>>(n, rs.as<int32_t>(), keys.as<unsigned long long>(),
@@ -1098,7 +1095,7 @@ int device_graph_from_edges(int64_t count, const int32_t* src, const int32_t* ds
         return fail(FBC_ERR_OOM, "device allocation failed");
     }
     fbc::gb_merge_kernel<<<grid_for(n), 256, 0, g.st>>>(n, rs.as<int32_t>(), keys.as<unsigned long long>(),
-                                                        dw.as<double>(), G->d_rp, G->d_adj, indeg.as<int32_t>(),
+                                                        dw, G->d_rp, G->d_adj, indeg.as<int32_t>(),
                                                         di + 2, (unsigned long long*)(di + 4), di + 1);
     fbc::gb_max_kernel<<<grid_for(n), 256, 0, g.st>>>(n, indeg.as<int32_t>(), di + 3);
     std::vector<int32_t> rp32((size_t)n + 1);
@@ -1131,6 +1128,75 @@ int device_graph_from_edges(int64_t count, const int32_t* src, const int32_t* ds
     }
     *out = guard.release();
     return FBC_OK;
+}
+
+// Edge list in host memory -> device CSR: upload, then device_csr_build.
+int device_graph_from_edges(int64_t count, const int32_t* src, const int32_t* dst, const double* w,
+                            fbc_graph* out) {
+    TmpBuf dsrc, ddst, dw;
+    FBC_CK(dsrc.ensure(sizeof(int32_t) * (size_t)count));
+    FBC_CK(ddst.ensure(sizeof(int32_t) * (size_t)count));
+    FBC_CK(dw.ensure(sizeof(double) * (size_t)count));
+    FBC_CK(cudaMemcpyAsync(dsrc.p, src, sizeof(int32_t) * (size_t)count, cudaMemcpyHostToDevice, g.st));
+    FBC_CK(cudaMemcpyAsync(ddst.p, dst, sizeof(int32_t) * (size_t)count, cudaMemcpyHostToDevice, g.st));
+    FBC_CK(cudaMemcpyAsync(dw.p, w, sizeof(double) * (size_t)count, cudaMemcpyHostToDevice, g.st));
+    return device_csr_build(count, dsrc.as<int32_t>(), ddst.as<int32_t>(), dw.as<double>(), out);
+}
+
+// Edge list -> CSR on the host (DirectedWeightedGraph.h:136-170): rows by source, each row
+// ascending by destination (the std::map order), a repeated pair's weights summed in input order.
+int host_graph_from_edges(int64_t count, const int32_t* src, const int32_t* dst, const double* w, fbc_graph* out) {
+    int32_t maxs = -1;
+    for (int64_t i = 0; i < count; ++i) {
+        if (!(w[i] > 0)) return fail(FBC_ERR_INVALID_ARG, "Edge weight must be greater than zero");
+        if (src[i] < 0 || dst[i] < 0) return fail(FBC_ERR_INVALID_ARG, "negative vertex id");
+        maxs = std::max(maxs, src[i]);
+    }
+    const int32_t n = maxs + 1;
+    std::vector<int64_t> idx((size_t)count);
+    std::iota(idx.begin(), idx.end(), 0);
+    std::stable_sort(idx.begin(), idx.end(), [&](int64_t a, int64_t b) {
+        return src[a] != src[b] ? src[a] < src[b] : dst[a] < dst[b];
+    });
+    std::vector<int64_t> rp((size_t)n + 1, 0);
+    std::vector<int32_t> col;
+    std::vector<double> ww;
+    col.reserve((size_t)count);
+    ww.reserve((size_t)count);
+    int32_t ps = -1, pd = -1;
+    for (int64_t k = 0; k < count; ++k) {
+        const int64_t i = idx[(size_t)k];
+        if (dst[i] >= n)
+            return fail(FBC_ERR_INVALID_ARG, "destination id " + std::to_string(dst[i]) +
+                                                 " is not below 1 + max source id");
+        if (src[i] == ps && dst[i] == pd) {
+            ww.back() += w[i];  // DirectedWeightedGraph.h:154-155: repeated pair, weights summed
+        } else {
+            col.push_back(dst[i]);
+            ww.push_back(w[i]);
+            rp[(size_t)src[i] + 1]++;
+            ps = src[i];
+            pd = dst[i];
+        }
+    }
+    for (int32_t v = 0; v < n; ++v) rp[(size_t)v + 1] += rp[(size_t)v];
+    return make_graph(n, std::move(rp), std::move(col), ww.data(), out);
+}
+
+// A weight token the device left to the host: operator>>(double&) of the classic locale on the
+// whole token, so overflow reads as the largest double with failbit set (the reference loop
+// then ends, DirectedWeightedGraph.h:83-86) and underflow as 0 or a subnormal.
+enum class TxHost { kValue, kStop, kNotPositive };
+TxHost tx_host_weight(const char* text, int64_t len, int64_t pos, double& v) {
+    int64_t end = pos;
+    while (end < len && !(text[end] == ' ' || (text[end] >= 9 && text[end] <= 13))) ++end;
+    std::istringstream in(std::string(text + pos, (size_t)(end - pos)));
+    in.imbue(std::locale::classic());
+    v = 0.0;
+    in >> v;
+    if (!(v > 0)) return TxHost::kNotPositive;
+    if (in.fail()) return TxHost::kStop;
+    return TxHost::kValue;
 }
 
 }  // namespace
@@ -1254,41 +1320,104 @@ int fbc_graph_from_edges(int64_t count, const int32_t* src, const int32_t* dst, 
         FBC_TRY(device_graph_from_edges(count, src, dst, w, out));
         if (*out) return FBC_OK;  // else a row too long for the device sort: the host path
     }
-    int32_t maxs = -1;
-    for (int64_t i = 0; i < count; ++i) {
-        if (!(w[i] > 0)) return fail(FBC_ERR_INVALID_ARG, "Edge weight must be greater than zero");
-        if (src[i] < 0 || dst[i] < 0) return fail(FBC_ERR_INVALID_ARG, "negative vertex id");
-        maxs = std::max(maxs, src[i]);
+    return host_graph_from_edges(count, src, dst, w, out);
+}
+
+int fbc_graph_from_text(const char* text, int64_t len, fbc_graph* out) {
+    std::lock_guard<std::recursive_mutex> lk(g_mu);
+    FBC_TRY(check_init());
+    if (!out || len < 0 || (len > 0 && !text)) return fail(FBC_ERR_INVALID_ARG, "null argument");
+    *out = nullptr;
+    if (len > (int64_t)INT32_MAX - 2 * fbc::kTxTile) return fail(FBC_ERR_RANGE, "edge-list text longer than 2 GiB");
+    // the device copy ends in at least one space, so every token scan stops inside it
+    const int64_t ntiles = (len + 1 + fbc::kTxTile - 1) / fbc::kTxTile;
+    const size_t padded = (size_t)ntiles * fbc::kTxTile;
+    TmpBuf dtext, cnt, toff, tok, dsrc, ddst, dw, find, slow, fix_i, fix_v;
+    FBC_CK(dtext.ensure(padded));
+    if (len > 0) FBC_CK(cudaMemcpyAsync(dtext.p, text, (size_t)len, cudaMemcpyHostToDevice, g.st));
+    FBC_CK(cudaMemsetAsync((char*)dtext.p + len, ' ', padded - (size_t)len, g.st));
+    FBC_CK(cnt.ensure(sizeof(int32_t) * (size_t)ntiles));
+    FBC_CK(toff.ensure(sizeof(int32_t) * ((size_t)ntiles + 1)));
+    const unsigned char* dt = (const unsigned char*)dtext.p;
+    const unsigned tgrid = (unsigned)std::min<int64_t>(ntiles, (int64_t)g.nsm * 8);
+    fbc::tx_count_kernel<<<tgrid, fbc::kTxThreads, 0, g.st>>>(ntiles, dt, cnt.as<int32_t>());
+    ++g_aux_launches;
+    FBC_CK(cudaGetLastError());
+    FBC_TRY(device_scan(cnt.as<int32_t>(), ntiles, toff.as<int32_t>()));
+    int32_t ntok = 0;
+    FBC_CK(cudaMemcpyAsync(&ntok, toff.as<int32_t>() + ntiles, sizeof(int32_t), cudaMemcpyDeviceToHost, g.st));
+    FBC_CK(cudaStreamSynchronize(g.st));
+    const int64_t nedges = ntok / 3;
+    FBC_CK(tok.ensure(sizeof(int32_t) * (size_t)std::max(ntok, 1)));
+    fbc::tx_starts_kernel<<<tgrid, fbc::kTxThreads, 0, g.st>>>(ntiles, dt, toff.as<int32_t>(), tok.as<int32_t>());
+    ++g_aux_launches;
+    FBC_CK(cudaGetLastError());
+    const size_t ne = (size_t)std::max<int64_t>(nedges, 1);
+    FBC_CK(dsrc.ensure(sizeof(int32_t) * ne));
+    FBC_CK(ddst.ensure(sizeof(int32_t) * ne));
+    FBC_CK(dw.ensure(sizeof(double) * ne));
+    FBC_CK(slow.ensure(sizeof(int2) * ne));
+    FBC_CK(find.ensure(sizeof(fbc::TxFind)));
+    fbc::TxFind hf{INT32_MAX, INT32_MAX, 0};
+    FBC_CK(cudaMemcpyAsync(find.p, &hf, sizeof(hf), cudaMemcpyHostToDevice, g.st));
+    if (nedges > 0) {
+        fbc::tx_edges_kernel<<<grid_for(nedges), 256, 0, g.st>>>(nedges, dt, tok.as<int32_t>(), dsrc.as<int32_t>(),
+                                                                ddst.as<int32_t>(), dw.as<double>(),
+                                                                find.as<fbc::TxFind>(), slow.as<int2>());
+        FBC_CK(cudaGetLastError());
     }
-    const int32_t n = maxs + 1;
-    std::vector<int64_t> idx((size_t)count);
-    std::iota(idx.begin(), idx.end(), 0);
-    std::stable_sort(idx.begin(), idx.end(), [&](int64_t a, int64_t b) {
-        return src[a] != src[b] ? src[a] < src[b] : dst[a] < dst[b];
-    });
-    std::vector<int64_t> rp((size_t)n + 1, 0);
-    std::vector<int32_t> col;
-    std::vector<double> ww;
-    col.reserve((size_t)count);
-    ww.reserve((size_t)count);
-    int32_t ps = -1, pd = -1;
-    for (int64_t k = 0; k < count; ++k) {
-        const int64_t i = idx[(size_t)k];
-        if (dst[i] >= n)
-            return fail(FBC_ERR_INVALID_ARG, "destination id " + std::to_string(dst[i]) +
-                                                 " is not below 1 + max source id");
-        if (src[i] == ps && dst[i] == pd) {
-            ww.back() += w[i];  // DirectedWeightedGraph.h:154-155: repeated pair, weights summed
-        } else {
-            col.push_back(dst[i]);
-            ww.push_back(w[i]);
-            rp[(size_t)src[i] + 1]++;
-            ps = src[i];
-            pd = dst[i];
+    FBC_CK(cudaMemcpyAsync(&hf, find.p, sizeof(hf), cudaMemcpyDeviceToHost, g.st));
+    FBC_CK(cudaStreamSynchronize(g.st));
+    // weights left to the host, and where reading ends (a weight that overflows a double)
+    int64_t stop = nedges, bad_w = hf.bad_w;
+    std::vector<int32_t> fi;
+    std::vector<double> fv;
+    if (hf.nslow > 0) {
+        std::vector<int2> sl((size_t)hf.nslow);
+        FBC_CK(cudaMemcpyAsync(sl.data(), slow.p, sizeof(int2) * sl.size(), cudaMemcpyDeviceToHost, g.st));
+        FBC_CK(cudaStreamSynchronize(g.st));
+        for (const int2& t : sl) {
+            double v = 0.0;
+            switch (tx_host_weight(text, len, t.y, v)) {
+                case TxHost::kValue: fi.push_back(t.x); fv.push_back(v); break;
+                case TxHost::kStop: stop = std::min<int64_t>(stop, t.x); break;
+                case TxHost::kNotPositive: bad_w = std::min<int64_t>(bad_w, t.x); break;
+            }
         }
     }
-    for (int32_t v = 0; v < n; ++v) rp[(size_t)v + 1] += rp[(size_t)v];
-    return make_graph(n, std::move(rp), std::move(col), ww.data(), out);
+    // the first finding in text order decides (an id before the weight of its triple); nothing
+    // after the end of reading counts
+    if (std::min<int64_t>(hf.bad_id, bad_w) <= stop) {
+        if (hf.bad_id <= bad_w)
+            return fail(FBC_ERR_INVALID_ARG, "edge " + std::to_string(hf.bad_id) + ": a vertex id is not a decimal int32");
+        return fail(FBC_ERR_INVALID_ARG, "Edge weight must be greater than zero (edge " + std::to_string(bad_w) + ")");
+    }
+    if (stop == nedges && ntok % 3 != 0)
+        return fail(FBC_ERR_INVALID_ARG, "the text ends inside an edge (" + std::to_string(ntok % 3) + " of 3 fields)");
+    if (!fi.empty()) {
+        FBC_CK(fix_i.ensure(sizeof(int32_t) * fi.size()));
+        FBC_CK(fix_v.ensure(sizeof(double) * fv.size()));
+        FBC_CK(cudaMemcpyAsync(fix_i.p, fi.data(), sizeof(int32_t) * fi.size(), cudaMemcpyHostToDevice, g.st));
+        FBC_CK(cudaMemcpyAsync(fix_v.p, fv.data(), sizeof(double) * fv.size(), cudaMemcpyHostToDevice, g.st));
+        fbc::tx_fix_kernel<<<grid_for((int64_t)fi.size()), 256, 0, g.st>>>((int32_t)fi.size(), fix_i.as<int32_t>(),
+                                                                           fix_v.as<double>(), dw.as<double>());
+        FBC_CK(cudaGetLastError());
+    }
+    const int64_t count = stop;
+    if (count > 0) {
+        FBC_TRY(device_csr_build(count, dsrc.as<int32_t>(), ddst.as<int32_t>(), dw.as<double>(), out));
+        if (*out) return FBC_OK;
+    }
+    // no edges, or a row too long for the device sort: the host build from the parsed arrays
+    std::vector<int32_t> hs((size_t)count), hd((size_t)count);
+    std::vector<double> hw((size_t)count);
+    if (count > 0) {
+        FBC_CK(cudaMemcpyAsync(hs.data(), dsrc.p, sizeof(int32_t) * hs.size(), cudaMemcpyDeviceToHost, g.st));
+        FBC_CK(cudaMemcpyAsync(hd.data(), ddst.p, sizeof(int32_t) * hd.size(), cudaMemcpyDeviceToHost, g.st));
+        FBC_CK(cudaMemcpyAsync(hw.data(), dw.p, sizeof(double) * hw.size(), cudaMemcpyDeviceToHost, g.st));
+        FBC_CK(cudaStreamSynchronize(g.st));
+    }
+    return host_graph_from_edges(count, hs.data(), hd.data(), hw.data(), out);
 }
 
 int fbc_graph_info(fbc_graph G, int32_t* n, int64_t* m) {

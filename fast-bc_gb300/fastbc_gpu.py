@@ -75,6 +75,7 @@ def _load():
         "fbc_get_option": ([C.c_char_p, P(i64)], C.c_int),
         "fbc_graph_upload": ([i32, vp, vp, vp, P(vp)], C.c_int),
         "fbc_graph_from_edges": ([i64, vp, vp, vp, P(vp)], C.c_int),
+        "fbc_graph_from_text": ([C.c_char_p, i64, P(vp)], C.c_int),
         "fbc_graph_info": ([vp, P(i32), P(i64)], C.c_int),
         "fbc_graph_download": ([vp, vp, vp, vp], C.c_int),
         "fbc_graph_free": ([vp], C.c_int),
@@ -177,9 +178,19 @@ class Graph:
         return cls.from_csr(rp, col, w.astype(np.float64))
 
     @classmethod
+    def from_text(cls, data: bytes) -> "Graph":
+        """Edge-list text ("src dst weight" triples, the file format fbc reads), tokenised and
+        parsed on the device with the reference parser's rules (fbc_graph_from_text)."""
+        init()
+        data = bytes(data)
+        h = C.c_void_p()
+        _ck(lib.fbc_graph_from_text(data, len(data), C.byref(h)))
+        return cls(h)
+
+    @classmethod
     def from_file(cls, path: str) -> "Graph":
-        a = np.loadtxt(path, ndmin=2)
-        return cls.from_edges(a[:, 0].astype(np.int32), a[:, 1].astype(np.int32), a[:, 2])
+        with open(path, "rb") as f:
+            return cls.from_text(f.read())
 
     def csr(self):
         rp = np.zeros(self.n + 1, np.int64)

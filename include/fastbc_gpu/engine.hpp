@@ -11,6 +11,8 @@
 #pragma once
 
 #include <cstdint>
+#include <fstream>
+#include <iterator>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -70,6 +72,31 @@ class DeviceGraph {
         d->n_ = (int32_t)n;
         d->m_ = rp[(size_t)n];
         return d;
+    }
+
+    // From the bytes of an edge-list file (the format fbc reads), parsed on the device.
+    static std::shared_ptr<DeviceGraph> from_text(const std::string& text, int device = 0) {
+        ensure_device(device);
+        auto d = std::make_shared<DeviceGraph>();
+        check(fbc_graph_from_text(text.data(), (int64_t)text.size(), &d->h_));
+        check(fbc_graph_info(d->h_, &d->n_, &d->m_));
+        return d;
+    }
+
+    static std::shared_ptr<DeviceGraph> from_file(const std::string& path, int device = 0) {
+        std::ifstream f(path, std::ios::binary);
+        if (!f) throw Error(FBC_ERR_INVALID_ARG, "cannot open " + path);
+        std::string text((std::istreambuf_iterator<char>(f)), std::istreambuf_iterator<char>());
+        return from_text(text, device);
+    }
+
+    // The CSR (rows ascending by destination, the forward stars' order), for building the host
+    // graph the rest of fbc works on.
+    void download_csr(std::vector<int64_t>& rp, std::vector<int32_t>& col, std::vector<double>& w) const {
+        rp.assign((size_t)n_ + 1, 0);
+        col.assign((size_t)m_, 0);
+        w.assign((size_t)m_, 0.0);
+        check(fbc_graph_download(h_, rp.data(), col.data(), w.data()));
     }
 
     fbc_graph handle() const { return h_; }

@@ -102,6 +102,16 @@ int fbc_graph_upload(int32_t n, const int64_t* row_ptr, const int32_t* col, cons
 int fbc_graph_from_edges(int64_t count, const int32_t* src, const int32_t* dst, const double* w,
                          fbc_graph* out);
 
+/* Device graph from edge-list text (the bytes of the file fbc reads,
+ * DirectedWeightedGraph(std::istream&), DirectedWeightedGraph.h:67-96): whitespace-separated
+ * triples "src dst weight", ids read as int and weights as double exactly as operator>> does
+ * (correctly rounded; a weight that overflows a double ends the reading there, as the
+ * reference's loop does), then the rules of fbc_graph_from_edges.  Tokenised and parsed on the
+ * device; len < 2 GiB.  FBC_ERR_INVALID_ARG for a weight <= 0 or not a number ("Edge weight
+ * must be greater than zero"), an id token that is not a decimal int32, or text that ends
+ * inside a triple (the last two are undefined behaviour in the reference). */
+int fbc_graph_from_text(const char* text, int64_t len, fbc_graph* out);
+
 int fbc_graph_info(fbc_graph g, int32_t* n, int64_t* m);
 /* Download the CSR (row_ptr[n+1], col[m], w[m]); any pointer may be NULL. */
 int fbc_graph_download(fbc_graph g, int64_t* row_ptr, int32_t* col, double* w);

@@ -15,6 +15,9 @@
 //   classes   <edges> <clusters> <out_prefix>       cluster evaluation + VertexInfoPivotSelector per
 //                                                   cluster (clusters file: one line per cluster,
 //                                                   "count v1 v2 ..."): exact classes' pivots/sizes
+//   graph     <edges> <out>                         DirectedWeightedGraph(std::istream&) alone: "n m",
+//                                                   then "src dst weight" per edge in forward-star
+//                                                   order, or "error <what()>" when it throws
 //   pins                                            the reference unit-test scenarios on DWGtext
 #define FASTBC_BRANDES_ENABLE_PIVOT_BORDER
 #define FASTBC_BRANDES_CLUSTERED_IGNORE_UNCONNECTED
@@ -82,6 +85,19 @@ static std::vector<std::vector<V>> read_clusters(const char* path) {
 int main(int argc, char** argv) {
     if (argc < 2) { std::fprintf(stderr, "usage: see header\n"); return 2; }
     std::string mode = argv[1];
+    if (mode == "graph" && argc == 4) {
+        std::FILE* o = std::fopen(argv[3], "w");
+        try {
+            auto g = load(argv[2]);
+            std::fprintf(o, "%zu %d\n", g->vertices().size(), (int)g->edges());
+            for (V v : g->vertices())
+                for (const auto& e : g->forwardStar(v)) std::fprintf(o, "%d %d %.17g\n", v, e.first, e.second);
+        } catch (const std::exception& e) {
+            std::fprintf(o, "error %s\n", e.what());
+        }
+        std::fclose(o);
+        return 0;
+    }
     if (mode == "exact" && argc == 4) {
         auto g = load(argv[2]);
         fastbc::brandes::ExactBrandesBC<V, W> bc;

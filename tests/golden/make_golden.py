@@ -15,9 +15,14 @@ oracle/_ref/ref_harness) single-threaded on the seeded workloads and stores:
                              2048x2048 grid: community id per vertex (int16; every
                              community's vertices are ascending, as the reference lists them)
   DWGtext.txt                the reference unit tests' 9-vertex fixture (copied)
+  text/<case>.txt, .out      edge-list texts in the formats operator>> accepts (layout, number
+                             forms, weights past a double's fast conversion, overflow ending the
+                             reading, rejected weights) and what DirectedWeightedGraph(istream&)
+                             made of each: "n m" and the forward stars, or "error <what()>"
 The clustered run takes about 15 minutes on one core, the 2048x2048 partition about a
 minute on eight.  Usage:
   python tests/golden/make_golden.py [--reuse DIR]   (DIR: outputs of an earlier harness run)
+  python tests/golden/make_golden.py --only text     (the text/ fixtures alone, seconds)
 """
 from __future__ import annotations
 
@@ -61,11 +66,68 @@ def parse_clusters(path):
     return flat(cv), flat(bv), flat(pv), flat(kv)
 
 
+def text_cases() -> dict:
+    """Edge-list texts whose reading is defined by the reference parser (every merged weight an
+    integer, which the GPU engine requires)."""
+    rng = np.random.default_rng(11)
+    cases = {
+        # tabs, runs of spaces, CRLF, blank lines, leading spaces, no final newline
+        "layout": b"  0 1 3\r\n1\t2\t4\n\n\n2   0 5\r\n\t 0 2 1\n1 0\t\t2",
+        # signs, leading zeros, points, exponents; repeated pairs summed (2.5 + 0.5, 10 + 2.5 + 0.5)
+        "numbers": (b"+0 1 +3\n001 2 3.\n2 0 .5e1\n0 2 2.50\n0 2 0.5\n1 0 1E+1\n1 0 250e-2\n"
+                    b"1 0 0.5\n2 1 0000.000100e4\n-0 3 7000e-3\n3 0 +.2e1\n"),
+        # more than 19 significant digits or powers of ten past 10^22
+        "long_weights": (b"0 1 1.0000000000000000000000001\n1 2 3000000000000000000000000000e-27\n"
+                         b"2 0 0.000000000000000000000000000000000000000007e42\n"
+                         b"0 2 2.99999999999999999999999999999\n2 1 40000000000000000000000e-22\n"
+                         b"1 0 6.000000000000000000000000000001\n1 1 1e0000000000000000000000000\n"),
+        # a weight past the largest double ends the reading; what follows is never read
+        "overflow_stops": b"0 1 2\n1 0 3\n1 0 1e400\n2 1 oops\n",
+        "zero_weight": b"0 1 2\n1 0 0\n1 1 1\n",
+        "negative_weight": b"0 1 2\n1 0 -3\n",
+        "word_weight": b"0 1 2\n1 0 abc\n",
+        "underflow_weight": b"0 1 2\n1 0 1e-400\n",
+    }
+    # a few thousand edges over 300 vertices, repeated pairs, random spacing and integer
+    # weights written in assorted forms
+    n, m = 300, 4000
+    src = rng.integers(0, n, m)
+    dst = rng.integers(0, n, m)
+    src[:n] = np.arange(n)  # every id a source, so n = 300
+    w = rng.integers(1, 50, m)
+    forms = [lambda x: b"%d" % x, lambda x: b"%d.0" % x, lambda x: b"+%d" % x,
+             lambda x: b"%.1fe1" % (x / 10), lambda x: b"%de-1" % (10 * x),
+             lambda x: b"%d.000000000000000000001" % x, lambda x: b"0%d." % x]
+    seps = [b" ", b"\t", b"  ", b" \t "]
+    ends = [b"\n", b"\r\n", b"\n\n", b" \n"]
+    out = []
+    for i in range(m):
+        f = forms[rng.integers(len(forms))]
+        sp = seps[rng.integers(len(seps))]
+        out.append(b"%d%s%d%s%s%s" % (src[i], sp, dst[i], sp, f(int(w[i])), ends[rng.integers(len(ends))]))
+    cases["mixed"] = b"".join(out)
+    return cases
+
+
+def text_goldens() -> None:
+    tdir = os.path.join(HERE, "text")
+    os.makedirs(tdir, exist_ok=True)
+    for name, data in text_cases().items():
+        p = os.path.join(tdir, name + ".txt")
+        with open(p, "wb") as f:
+            f.write(data)
+        run("graph", p, os.path.join(tdir, name + ".out"))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reuse", default=None)
+    ap.add_argument("--only", choices=["text"], default=None)
     a = ap.parse_args()
     subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref", f"REF={REF}"], check=True)
+    text_goldens()
+    if a.only == "text":
+        return
     shutil.copy(os.path.join(REF, "libfastbc", "test", "DWGtext.txt"), os.path.join(HERE, "DWGtext.txt"))
     work = a.reuse or tempfile.mkdtemp()
     g32 = os.path.join(work, "grid32.txt")

@@ -1,0 +1,34 @@
+"""The edge-list text oracle pinned to the reference's own parser (DirectedWeightedGraph(std::
+istream&), DirectedWeightedGraph.h:67-96) on the fixtures of tests/golden/text (CPU only)."""
+import numpy as np
+import pytest
+
+import text_cases
+import text_oracle as to
+
+
+@pytest.mark.parametrize("name", text_cases.cases())
+def test_oracle_reads_like_the_reference(name):
+    text, want = text_cases.load(name)
+    if isinstance(want, str):
+        assert want == "Edge weight must be greater than zero"
+        with pytest.raises(to.TextError) as e:
+            to.parse_edge_text(text)
+        assert e.value.kind == "weight"
+        return
+    rp, col, w = to.csr_from_edges(*to.parse_edge_text(text))
+    assert np.array_equal(rp, want[0]) and np.array_equal(col, want[1])
+    assert np.array_equal(w, want[2])  # exact: both sides are correctly rounded
+
+
+def test_oracle_undefined_cases_are_errors():
+    for text, kind, edge in [(b"0 1 2\n1 0", "incomplete", 1), (b"0 1 2\n1.5 0 3\n", "id", 1),
+                             (b"0 99999999999 2\n", "id", 0), (b"0 1 2x\n", "weight", 0),
+                             (b"0 1 2\n1 0 1e400\nx y z w\n", None, None)]:
+        if kind is None:
+            s, d, w = to.parse_edge_text(text)
+            assert list(s) == [0] and list(w) == [2.0]
+            continue
+        with pytest.raises(to.TextError) as e:
+            to.parse_edge_text(text)
+        assert (e.value.kind, e.value.edge) == (kind, edge)
