@@ -141,6 +141,9 @@ struct fbc_graph_s {
     double meanw = 1.0;
     int32_t* d_rp = nullptr;
     int2* d_adj = nullptr;
+    // host copy of the CSR (bisection order, downloads, debug predecessor counts); a graph
+    // built on the device fetches it on first use
+    bool host_ok = true;
     std::vector<int64_t> h_rp;
     std::vector<int32_t> h_col;
     std::vector<int32_t> h_w;
@@ -332,9 +335,31 @@ std::vector<int32_t> bisection_order(int32_t n, const std::vector<int64_t>& rp, 
     return nw;
 }
 
+// The host copy of a device-built graph's CSR, downloaded once.
+int ensure_host_csr(fbc_graph_s* G) {
+    if (G->host_ok) return FBC_OK;
+    const int32_t n = G->n;
+    std::vector<int32_t> rp32((size_t)n + 1);
+    std::vector<int2> adj((size_t)std::max<int64_t>(G->m, 1));
+    FBC_CK(cudaMemcpyAsync(rp32.data(), G->d_rp, sizeof(int32_t) * rp32.size(), cudaMemcpyDeviceToHost, g.st));
+    if (G->m > 0)
+        FBC_CK(cudaMemcpyAsync(adj.data(), G->d_adj, sizeof(int2) * (size_t)G->m, cudaMemcpyDeviceToHost, g.st));
+    FBC_CK(cudaStreamSynchronize(g.st));
+    G->h_rp.assign(rp32.begin(), rp32.end());
+    G->h_col.resize((size_t)G->m);
+    G->h_w.resize((size_t)G->m);
+    for (int64_t k = 0; k < G->m; ++k) {
+        G->h_col[k] = adj[k].x;
+        G->h_w[k] = adj[k].y;
+    }
+    G->host_ok = true;
+    return FBC_OK;
+}
+
 // Build (once) the relabelled device CSR of a graph: rows ascending in the new ids.
 int ensure_order(fbc_graph_s* G) {
     if (G->ord_built) return FBC_OK;
+    FBC_TRY(ensure_host_csr(G));
     const int32_t n = G->n;
     std::vector<int32_t> nw = bisection_order(n, G->h_rp, G->h_col, 16);
     std::vector<int32_t> inv((size_t)std::max(n, 1));
@@ -1098,13 +1123,8 @@ int device_csr_build(int64_t count, const int32_t* dsrc, const int32_t* ddst, co
                                                         dw, G->d_rp, G->d_adj, indeg.as<int32_t>(),
                                                         di + 2, (unsigned long long*)(di + 4), di + 1);
     fbc::gb_max_kernel<<<grid_for(n), 256, 0, g.st>>>(n, indeg.as<int32_t>(), di + 3);
-    std::vector<int32_t> rp32((size_t)n + 1);
-    std::vector<int2> adj((size_t)medges);
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaMemcpyAsync(hi, ints.p, sizeof(hi), cudaMemcpyDeviceToHost, g.st);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(rp32.data(), G->d_rp, sizeof(int32_t) * rp32.size(), cudaMemcpyDeviceToHost, g.st);
-    if (e == cudaSuccess && medges > 0)
-        e = cudaMemcpyAsync(adj.data(), G->d_adj, sizeof(int2) * adj.size(), cudaMemcpyDeviceToHost, g.st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(g.st);
     if (e != cudaSuccess) { drop(); return fail(FBC_ERR_CUDA, std::string("graph build: ") + cudaGetErrorString(e)); }
     if (hi[1] & fbc::kGbNonInt) { drop(); return fail(FBC_ERR_RANGE, "edge weights must be integers below 2^31"); }
@@ -1118,14 +1138,7 @@ int device_csr_build(int64_t count, const int32_t* dsrc, const int32_t* ddst, co
         drop();
         return fail(FBC_ERR_RANGE, "n * max_weight exceeds the int32 distance range");
     }
-    G->h_rp.resize((size_t)n + 1);
-    for (int32_t v = 0; v <= n; ++v) G->h_rp[v] = rp32[v];
-    G->h_col.resize((size_t)medges);
-    G->h_w.resize((size_t)medges);
-    for (int32_t k = 0; k < medges; ++k) {
-        G->h_col[k] = adj[k].x;
-        G->h_w[k] = adj[k].y;
-    }
+    G->host_ok = false;  // the host copy is fetched when something needs it
     *out = guard.release();
     return FBC_OK;
 }
@@ -1323,51 +1336,68 @@ int fbc_graph_from_edges(int64_t count, const int32_t* src, const int32_t* dst, 
     return host_graph_from_edges(count, src, dst, w, out);
 }
 
-int fbc_graph_from_text(const char* text, int64_t len, fbc_graph* out) {
+int fbc_graph_from_text(const char* text, int64_t len, fbc_graph* out, fbc_stats* st) {
     std::lock_guard<std::recursive_mutex> lk(g_mu);
     FBC_TRY(check_init());
     if (!out || len < 0 || (len > 0 && !text)) return fail(FBC_ERR_INVALID_ARG, "null argument");
     *out = nullptr;
+    if (st) std::memset(st, 0, sizeof(*st));
+    const double t0 = now_ms();
     if (len > (int64_t)INT32_MAX - 2 * fbc::kTxTile) return fail(FBC_ERR_RANGE, "edge-list text longer than 2 GiB");
     // the device copy ends in at least one space, so every token scan stops inside it
     const int64_t ntiles = (len + 1 + fbc::kTxTile - 1) / fbc::kTxTile;
     const size_t padded = (size_t)ntiles * fbc::kTxTile;
+    // capacities from the length alone (a token and its separator take two bytes, an edge six),
+    // so the passes run back to back with no host round trip
+    const int64_t tok_cap = (len + 1) / 2 + 1, edge_cap = (len + 1) / 6 + 1;
     TmpBuf dtext, cnt, toff, tok, dsrc, ddst, dw, find, slow, fix_i, fix_v;
     FBC_CK(dtext.ensure(padded));
-    if (len > 0) FBC_CK(cudaMemcpyAsync(dtext.p, text, (size_t)len, cudaMemcpyHostToDevice, g.st));
-    FBC_CK(cudaMemsetAsync((char*)dtext.p + len, ' ', padded - (size_t)len, g.st));
     FBC_CK(cnt.ensure(sizeof(int32_t) * (size_t)ntiles));
     FBC_CK(toff.ensure(sizeof(int32_t) * ((size_t)ntiles + 1)));
-    const unsigned char* dt = (const unsigned char*)dtext.p;
-    const unsigned tgrid = (unsigned)std::min<int64_t>(ntiles, (int64_t)g.nsm * 8);
-    fbc::tx_count_kernel<<<tgrid, fbc::kTxThreads, 0, g.st>>>(ntiles, dt, cnt.as<int32_t>());
-    ++g_aux_launches;
-    FBC_CK(cudaGetLastError());
-    FBC_TRY(device_scan(cnt.as<int32_t>(), ntiles, toff.as<int32_t>()));
-    int32_t ntok = 0;
-    FBC_CK(cudaMemcpyAsync(&ntok, toff.as<int32_t>() + ntiles, sizeof(int32_t), cudaMemcpyDeviceToHost, g.st));
-    FBC_CK(cudaStreamSynchronize(g.st));
-    const int64_t nedges = ntok / 3;
-    FBC_CK(tok.ensure(sizeof(int32_t) * (size_t)std::max(ntok, 1)));
-    fbc::tx_starts_kernel<<<tgrid, fbc::kTxThreads, 0, g.st>>>(ntiles, dt, toff.as<int32_t>(), tok.as<int32_t>());
-    ++g_aux_launches;
-    FBC_CK(cudaGetLastError());
-    const size_t ne = (size_t)std::max<int64_t>(nedges, 1);
-    FBC_CK(dsrc.ensure(sizeof(int32_t) * ne));
-    FBC_CK(ddst.ensure(sizeof(int32_t) * ne));
-    FBC_CK(dw.ensure(sizeof(double) * ne));
-    FBC_CK(slow.ensure(sizeof(int2) * ne));
+    FBC_CK(tok.ensure(sizeof(int32_t) * (size_t)tok_cap));
+    FBC_CK(dsrc.ensure(sizeof(int32_t) * (size_t)edge_cap));
+    FBC_CK(ddst.ensure(sizeof(int32_t) * (size_t)edge_cap));
+    FBC_CK(dw.ensure(sizeof(double) * (size_t)edge_cap));
+    FBC_CK(slow.ensure(sizeof(int2) * (size_t)edge_cap));
     FBC_CK(find.ensure(sizeof(fbc::TxFind)));
+    if (len > 0) FBC_CK(cudaMemcpyAsync(dtext.p, text, (size_t)len, cudaMemcpyHostToDevice, g.st));
+    FBC_CK(cudaMemsetAsync((char*)dtext.p + len, ' ', padded - (size_t)len, g.st));
     fbc::TxFind hf{INT32_MAX, INT32_MAX, 0};
     FBC_CK(cudaMemcpyAsync(find.p, &hf, sizeof(hf), cudaMemcpyHostToDevice, g.st));
-    if (nedges > 0) {
-        fbc::tx_edges_kernel<<<grid_for(nedges), 256, 0, g.st>>>(nedges, dt, tok.as<int32_t>(), dsrc.as<int32_t>(),
-                                                                ddst.as<int32_t>(), dw.as<double>(),
-                                                                find.as<fbc::TxFind>(), slow.as<int2>());
-        FBC_CK(cudaGetLastError());
+    cudaEvent_t ev[2];
+    FBC_CK(cudaEventCreate(&ev[0]));
+    FBC_CK(cudaEventCreate(&ev[1]));
+    cudaEventRecord(ev[0], g.st);
+    const unsigned char* dt = (const unsigned char*)dtext.p;
+    const unsigned tgrid = (unsigned)std::min<int64_t>(ntiles, (int64_t)g.nsm * 8);
+    const int aux0 = g_aux_launches;
+    fbc::tx_count_kernel<<<tgrid, fbc::kTxThreads, 0, g.st>>>(ntiles, dt, cnt.as<int32_t>());
+    int rc = device_scan(cnt.as<int32_t>(), ntiles, toff.as<int32_t>());
+    if (rc == FBC_OK) {
+        fbc::tx_starts_kernel<<<tgrid, fbc::kTxThreads, 0, g.st>>>(ntiles, dt, toff.as<int32_t>(), tok.as<int32_t>());
+        fbc::tx_edges_kernel<<<grid_for(edge_cap), 256, 0, g.st>>>(toff.as<int32_t>() + ntiles, dt, tok.as<int32_t>(),
+                                                                  dsrc.as<int32_t>(), ddst.as<int32_t>(), dw.as<double>(),
+                                                                  find.as<fbc::TxFind>(), slow.as<int2>());
     }
-    FBC_CK(cudaMemcpyAsync(&hf, find.p, sizeof(hf), cudaMemcpyDeviceToHost, g.st));
-    FBC_CK(cudaStreamSynchronize(g.st));
+    cudaEventRecord(ev[1], g.st);
+    int32_t ntok = 0;
+    cudaError_t ce = cudaGetLastError();
+    if (ce == cudaSuccess) ce = cudaMemcpyAsync(&hf, find.p, sizeof(hf), cudaMemcpyDeviceToHost, g.st);
+    if (ce == cudaSuccess)
+        ce = cudaMemcpyAsync(&ntok, toff.as<int32_t>() + ntiles, sizeof(int32_t), cudaMemcpyDeviceToHost, g.st);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(g.st);
+    float parse_ms = 0.f;
+    if (ce == cudaSuccess) cudaEventElapsedTime(&parse_ms, ev[0], ev[1]);
+    cudaEventDestroy(ev[0]);
+    cudaEventDestroy(ev[1]);
+    if (rc != FBC_OK) return rc;
+    if (ce != cudaSuccess) return fail(FBC_ERR_CUDA, std::string("text parse: ") + cudaGetErrorString(ce));
+    if (st) {
+        st->kernel_ms = parse_ms;
+        st->launches = 2 + (g_aux_launches - aux0);  // count, starts, and the scan and edges kernels
+        st->h2d_bytes = len;
+    }
+    const int64_t nedges = ntok / 3;
     // weights left to the host, and where reading ends (a weight that overflows a double)
     int64_t stop = nedges, bad_w = hf.bad_w;
     std::vector<int32_t> fi;
@@ -1406,7 +1436,13 @@ int fbc_graph_from_text(const char* text, int64_t len, fbc_graph* out) {
     const int64_t count = stop;
     if (count > 0) {
         FBC_TRY(device_csr_build(count, dsrc.as<int32_t>(), ddst.as<int32_t>(), dw.as<double>(), out));
-        if (*out) return FBC_OK;
+        if (*out) {
+            if (st) {
+                st->wall_ms = now_ms() - t0;
+                st->d2h_bytes = (int64_t)sizeof(fbc::TxFind) + 4 + 24;  // findings, token count, build summary
+            }
+            return FBC_OK;
+        }
     }
     // no edges, or a row too long for the device sort: the host build from the parsed arrays
     std::vector<int32_t> hs((size_t)count), hd((size_t)count);
@@ -1417,7 +1453,9 @@ int fbc_graph_from_text(const char* text, int64_t len, fbc_graph* out) {
         FBC_CK(cudaMemcpyAsync(hw.data(), dw.p, sizeof(double) * hw.size(), cudaMemcpyDeviceToHost, g.st));
         FBC_CK(cudaStreamSynchronize(g.st));
     }
-    return host_graph_from_edges(count, hs.data(), hd.data(), hw.data(), out);
+    FBC_TRY(host_graph_from_edges(count, hs.data(), hd.data(), hw.data(), out));
+    if (st) st->wall_ms = now_ms() - t0;
+    return FBC_OK;
 }
 
 int fbc_graph_info(fbc_graph G, int32_t* n, int64_t* m) {
@@ -1428,7 +1466,10 @@ int fbc_graph_info(fbc_graph G, int32_t* n, int64_t* m) {
 }
 
 int fbc_graph_download(fbc_graph G, int64_t* row_ptr, int32_t* col, double* w) {
+    std::lock_guard<std::recursive_mutex> lk(g_mu);
     if (!G) return fail(FBC_ERR_INVALID_ARG, "null graph");
+    FBC_TRY(check_init());
+    FBC_TRY(ensure_host_csr(G));
     if (row_ptr) std::copy(G->h_rp.begin(), G->h_rp.end(), row_ptr);
     if (col) std::copy(G->h_col.begin(), G->h_col.end(), col);
     if (w)
@@ -1948,6 +1989,7 @@ int fbc_sssp_debug(fbc_graph G, int32_t source, int32_t* out_dist, uint64_t* out
     if (out_sigma) FBC_CK(cudaMemcpy(out_sigma, P.dbg_sig, 8 * n, cudaMemcpyDeviceToHost));
     if (out_delta) FBC_CK(cudaMemcpy(out_delta, P.dbg_dlt, 8 * n, cudaMemcpyDeviceToHost));
     if (out_npred) {
+        FBC_TRY(ensure_host_csr(G));
         std::fill(out_npred, out_npred + n, 0);
         for (int32_t v = 0; v < G->n; ++v) {
             if (dist[v] < 0) continue;

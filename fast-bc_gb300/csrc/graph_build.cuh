@@ -100,8 +100,11 @@ __global__ void gb_merge_kernel(int32_t n, const int32_t* __restrict__ rs, const
         }
     }
     mw = __reduce_max_sync(0xffffffffu, mw);
-    if ((threadIdx.x & 31) == 0) atomicMax(maxw, mw);
-    atomicAdd(sumw, sw);
+    for (int d = 16; d > 0; d >>= 1) sw += __shfl_down_sync(0xffffffffu, sw, d);
+    if ((threadIdx.x & 31) == 0) {
+        atomicMax(maxw, mw);
+        atomicAdd(sumw, sw);  // one per warp: a per-thread add to one word serialises
+    }
 }
 
 __global__ void gb_max_kernel(int32_t n, const int32_t* __restrict__ x, int* out) {

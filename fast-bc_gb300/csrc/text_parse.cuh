@@ -189,9 +189,12 @@ __device__ __forceinline__ int tx_weight(const unsigned char* __restrict__ s, do
     return 0;
 }
 
-__global__ void tx_edges_kernel(int64_t nedges, const unsigned char* __restrict__ text, const int32_t* __restrict__ tok,
-                                int32_t* __restrict__ src, int32_t* __restrict__ dst, double* __restrict__ w,
-                                TxFind* find, int2* slow) {
+// one thread per triple; the token count comes from the scan (*ntok), so no host round trip
+// sits between the passes
+__global__ void tx_edges_kernel(const int32_t* __restrict__ ntok, const unsigned char* __restrict__ text,
+                                const int32_t* __restrict__ tok, int32_t* __restrict__ src, int32_t* __restrict__ dst,
+                                double* __restrict__ w, TxFind* find, int2* slow) {
+    const int64_t nedges = *ntok / 3;
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < nedges; e += (int64_t)gridDim.x * blockDim.x) {
         const int32_t ps = tok[3 * e], pd = tok[3 * e + 1], pw = tok[3 * e + 2];
         int32_t a = 0, b = 0;

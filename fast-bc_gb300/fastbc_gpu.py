@@ -75,7 +75,7 @@ def _load():
         "fbc_get_option": ([C.c_char_p, P(i64)], C.c_int),
         "fbc_graph_upload": ([i32, vp, vp, vp, P(vp)], C.c_int),
         "fbc_graph_from_edges": ([i64, vp, vp, vp, P(vp)], C.c_int),
-        "fbc_graph_from_text": ([C.c_char_p, i64, P(vp)], C.c_int),
+        "fbc_graph_from_text": ([C.c_char_p, i64, P(vp), P(Stats)], C.c_int),
         "fbc_graph_info": ([vp, P(i32), P(i64)], C.c_int),
         "fbc_graph_download": ([vp, vp, vp, vp], C.c_int),
         "fbc_graph_free": ([vp], C.c_int),
@@ -178,13 +178,13 @@ class Graph:
         return cls.from_csr(rp, col, w.astype(np.float64))
 
     @classmethod
-    def from_text(cls, data: bytes) -> "Graph":
+    def from_text(cls, data: bytes, stats: Stats | None = None) -> "Graph":
         """Edge-list text ("src dst weight" triples, the file format fbc reads), tokenised and
         parsed on the device with the reference parser's rules (fbc_graph_from_text)."""
         init()
         data = bytes(data)
         h = C.c_void_p()
-        _ck(lib.fbc_graph_from_text(data, len(data), C.byref(h)))
+        _ck(lib.fbc_graph_from_text(data, len(data), C.byref(h), _stats(stats)))
         return cls(h)
 
     @classmethod

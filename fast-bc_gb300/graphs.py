@@ -72,9 +72,34 @@ class EdgeList:
 
     def write(self, path: str) -> None:
         """Write the ``src dst w`` text form read by the reference ``fbc``."""
-        arr = np.stack([self.src.astype(np.int64), self.dst.astype(np.int64),
-                        self.w.astype(np.int64)], axis=1)
-        np.savetxt(path, arr, fmt="%d", delimiter=" ")
+        with open(path, "wb") as f:
+            f.write(self.text())
+
+    def text(self) -> bytes:
+        """The ``src dst w`` lines (decimal, one space, "\n") as bytes, formatted with array
+        operations: every number is written into a fixed-width field of digit bytes (as wide as
+        its column's largest value), and the unused leading positions are dropped."""
+        cols = [self.src, self.dst, self.w]
+        widths = [len(str(int(x.max()))) + 1 if x.size else 2 for x in cols]
+        m, tot = self.m, sum(widths)
+        buf = np.empty((m, tot), np.uint8)
+        keep = np.empty((m, tot), bool)
+        base = 0
+        for c, x in enumerate(cols):
+            y = x.astype(np.int32)
+            assert y.size == 0 or y.min() >= 0
+            wd = widths[c]
+            started = np.ones(m, bool)  # the lowest digit is always written
+            for k in range(wd - 1):  # digit k from the right
+                pos = base + wd - 2 - k
+                buf[:, pos] = 48 + (y % 10).astype(np.uint8)
+                keep[:, pos] = started
+                y = y // 10
+                started = y > 0
+            buf[:, base + wd - 1] = 32 if c < 2 else 10
+            keep[:, base + wd - 1] = True
+            base += wd
+        return buf[keep].tobytes()
 
     def csr(self):
         """CSR arrays (row_ptr int64[n+1], col int32[m], w int32[m]); neighbours ascending."""

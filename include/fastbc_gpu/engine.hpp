@@ -78,7 +78,7 @@ class DeviceGraph {
     static std::shared_ptr<DeviceGraph> from_text(const std::string& text, int device = 0) {
         ensure_device(device);
         auto d = std::make_shared<DeviceGraph>();
-        check(fbc_graph_from_text(text.data(), (int64_t)text.size(), &d->h_));
+        check(fbc_graph_from_text(text.data(), (int64_t)text.size(), &d->h_, nullptr));
         check(fbc_graph_info(d->h_, &d->n_, &d->m_));
         return d;
     }

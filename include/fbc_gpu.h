@@ -109,8 +109,10 @@ int fbc_graph_from_edges(int64_t count, const int32_t* src, const int32_t* dst, 
  * reference's loop does), then the rules of fbc_graph_from_edges.  Tokenised and parsed on the
  * device; len < 2 GiB.  FBC_ERR_INVALID_ARG for a weight <= 0 or not a number ("Edge weight
  * must be greater than zero"), an id token that is not a decimal int32, or text that ends
- * inside a triple (the last two are undefined behaviour in the reference). */
-int fbc_graph_from_text(const char* text, int64_t len, fbc_graph* out);
+ * inside a triple (the last two are undefined behaviour in the reference).
+ * st (optional): kernel_ms = device time of the tokenising and parsing kernels, wall_ms = the
+ * whole call (copy, parse, CSR build, host mirror), h2d/d2h bytes, launches of the parse. */
+int fbc_graph_from_text(const char* text, int64_t len, fbc_graph* out, fbc_stats* st);
 
 int fbc_graph_info(fbc_graph g, int32_t* n, int64_t* m);
 /* Download the CSR (row_ptr[n+1], col[m], w[m]); any pointer may be NULL. */

@@ -19,7 +19,9 @@ Pinned against the reference's own parser on the fixtures in tests/golden/text/.
 """
 from __future__ import annotations
 
+import ctypes as C
 import math
+import os
 import re
 
 import numpy as np
@@ -90,3 +92,55 @@ def csr_from_edges(src, dst, w):
             rp[key[0] + 1] += 1
             prev = key
     return np.cumsum(rp), np.array(col, np.int32), np.array(ww, np.float64)
+
+
+# the same reading in C (text_oracle.c, in liboracle.so): fast enough for full-size texts and
+# for the CPU baseline of the device parser
+_KINDS = {1: "weight", 2: "id", 3: "incomplete"}
+_clib = None
+
+
+def _c():
+    global _clib
+    if _clib is None:
+        lib = C.CDLL(os.path.join(os.path.dirname(os.path.abspath(__file__)), "liboracle.so"))
+        i64, vp = C.c_int64, C.c_void_p
+        lib.orc_parse_text.argtypes = [C.c_char_p, i64, vp, vp, vp, i64, C.POINTER(i64), C.POINTER(i64)]
+        lib.orc_parse_text.restype = C.c_int
+        lib.orc_csr_from_edges.argtypes = [i64, vp, vp, vp, C.c_int32, vp, vp, vp]
+        lib.orc_csr_from_edges.restype = i64
+        _clib = lib
+    return _clib
+
+
+def _p(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def parse_edge_text_c(data: bytes):
+    data = bytes(data)
+    cap = max(1, data.count(b"\n") + 1, len(data) // 6 + 1)  # every edge needs at least 6 bytes
+    src = np.empty(cap, np.int32)
+    dst = np.empty(cap, np.int32)
+    w = np.empty(cap, np.float64)
+    cnt, edge = C.c_int64(), C.c_int64()
+    rc = _c().orc_parse_text(data, len(data), _p(src), _p(dst), _p(w), cap, C.byref(cnt), C.byref(edge))
+    if rc != 0:
+        if rc < 0:
+            raise MemoryError("edge capacity")
+        raise TextError(_KINDS[rc], int(edge.value))
+    k = int(cnt.value)
+    return src[:k], dst[:k], w[:k]
+
+
+def csr_from_edges_c(src, dst, w):
+    src = np.ascontiguousarray(src, np.int32)
+    dst = np.ascontiguousarray(dst, np.int32)
+    w = np.ascontiguousarray(w, np.float64)
+    n = int(src.max()) + 1 if src.size else 0
+    rp = np.zeros(n + 1, np.int64)
+    col = np.empty(max(src.size, 1), np.int32)
+    ww = np.empty(max(src.size, 1), np.float64)
+    m = _c().orc_csr_from_edges(src.size, _p(src), _p(dst), _p(w), n, _p(rp), _p(col), _p(ww))
+    assert m >= 0
+    return rp, col[:m], ww[:m]

@@ -32,3 +32,33 @@ def test_oracle_undefined_cases_are_errors():
         with pytest.raises(to.TextError) as e:
             to.parse_edge_text(text)
         assert (e.value.kind, e.value.edge) == (kind, edge)
+
+
+@pytest.mark.parametrize("name", text_cases.cases())
+def test_c_oracle_reads_like_the_reference(name):
+    text, want = text_cases.load(name)
+    if isinstance(want, str):
+        with pytest.raises(to.TextError) as e:
+            to.parse_edge_text_c(text)
+        assert e.value.kind == "weight"
+        return
+    got = to.csr_from_edges_c(*to.parse_edge_text_c(text))
+    assert all(np.array_equal(a, b) for a, b in zip(got, want))
+
+
+def test_c_oracle_matches_python_oracle():
+    rng = np.random.default_rng(9)
+    toks = [b"0", b"17", b"+3", b"-2", b"1.5", b"2.", b".5e1", b"1e400", b"1e-400", b"x", b"00",
+            b"3e", b"99999999999", b"4.0000000000000000000000001"]
+    for trial in range(300):
+        k = int(rng.integers(0, 40))
+        parts = [toks[i] for i in rng.integers(0, len(toks), k)]
+        seps = [(b" ", b"\n", b"\t", b"\r\n")[i] for i in rng.integers(0, 4, k)]
+        text = b"".join(p + s for p, s in zip(parts, seps))
+        outs = []
+        for f in (to.parse_edge_text, to.parse_edge_text_c):
+            try:
+                outs.append(tuple(a.tolist() for a in f(text)))
+            except to.TextError as e:
+                outs.append((e.kind, e.edge))
+        assert outs[0] == outs[1], text
