@@ -98,6 +98,7 @@ struct Options {
     int64_t csr_device_min_m = 65536;  // edge lists of at least this many edges are built on the device
     int64_t wide_threads = 512;        // block size of the wide frontier kernel (<= 512)
     int64_t debug_sched = FBC_SCHED_PLAIN;  // schedule used by fbc_sssp_debug
+    int64_t scratch_keep_mb = 8192;  // per-call scratch the memory pool keeps for later calls
 };
 
 // A persistent workspace of equally sized slots.  Slot headers keep stamp counters, so a
@@ -116,6 +117,7 @@ struct Ctx {
     int nsm = 0;
     int smem_optin = 0;
     cudaStream_t st = nullptr;
+    cudaMemPool_t pool = nullptr;  // per-call scratch (TmpBuf), stream-ordered on st
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, evm = nullptr;
     Options opt;
     DBuf retry, segs, units_b, units_w, chunks, crp, cadj, cgid, cbord, bc, bdist, bsig, ctr, dbg;
@@ -1045,10 +1047,37 @@ int prepare_clusters(const fbc_graph_s* G, int32_t nclusters, const int64_t* cof
 }
 
 // A device buffer released when it goes out of scope (temporaries of a graph build).
-struct TmpBuf : DBuf {
+// Scratch of one call, allocated from the library's memory pool in the order of the library
+// stream and freed the same way (no device-wide synchronisation of cudaFree; the pool keeps up
+// to scratch_keep_mb of it for the next call).
+struct TmpBuf {
+    void* p = nullptr;
+    size_t cap = 0;
     TmpBuf() = default;
     TmpBuf(const TmpBuf&) = delete;
-    ~TmpBuf() { release(); }
+    TmpBuf& operator=(const TmpBuf&) = delete;
+    ~TmpBuf() {
+        if (p) cudaFreeAsync(p, g.st);
+    }
+    cudaError_t ensure(size_t bytes, bool zero = false) {
+        if (p && bytes <= cap) return cudaSuccess;
+        if (p) cudaFreeAsync(p, g.st);
+        p = nullptr;
+        cap = 0;
+        const size_t want = std::max<size_t>(bytes, 256);
+        cudaError_t e = cudaMallocFromPoolAsync(&p, want, g.pool, g.st);
+        if (e != cudaSuccess) {
+            p = nullptr;
+            return e;
+        }
+        cap = want;
+        if (zero) return cudaMemsetAsync(p, 0, want, g.st);
+        return cudaSuccess;
+    }
+    template <class T>
+    T* as() const {
+        return (T*)p;
+    }
 };
 
 // Edge list already on the device -> device CSR (graph_build.cuh).  Returns FBC_OK with *out
@@ -1238,6 +1267,13 @@ int fbc_gpu_init(int device) {
     FBC_CK(cudaEventCreate(&g.ev0));
     FBC_CK(cudaEventCreate(&g.ev1));
     FBC_CK(cudaEventCreate(&g.evm));
+    cudaMemPoolProps props{};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = device;
+    FBC_CK(cudaMemPoolCreate(&g.pool, &props));
+    uint64_t keep = (uint64_t)g.opt.scratch_keep_mb << 20;
+    FBC_CK(cudaMemPoolSetAttribute(g.pool, cudaMemPoolAttrReleaseThreshold, &keep));
     g.dev = device;
     g.init = true;
     return FBC_OK;
@@ -1258,6 +1294,9 @@ int fbc_gpu_shutdown(void) {
     cudaEventDestroy(g.ev0);
     cudaEventDestroy(g.ev1);
     cudaEventDestroy(g.evm);
+    cudaStreamSynchronize(g.st);
+    cudaMemPoolDestroy(g.pool);
+    g.pool = nullptr;
     cudaStreamDestroy(g.st);
     g.init = false;
     return FBC_OK;
@@ -1283,6 +1322,13 @@ int fbc_set_option(const char* key, int64_t value) {
         g.opt.group = value;
     }
     else if (k == "debug_sched") g.opt.debug_sched = value ? FBC_SCHED_BATCHED : FBC_SCHED_PLAIN;
+    else if (k == "scratch_keep_mb") {
+        g.opt.scratch_keep_mb = std::max<int64_t>(0, value);
+        if (g.pool) {
+            uint64_t keep = (uint64_t)g.opt.scratch_keep_mb << 20;
+            cudaMemPoolSetAttribute(g.pool, cudaMemPoolAttrReleaseThreshold, &keep);
+        }
+    }
     else return fail(FBC_ERR_INVALID_ARG, "unknown option " + k);
     return FBC_OK;
 }
@@ -1304,6 +1350,7 @@ int fbc_get_option(const char* key, int64_t* value) {
     else if (k == "csr_device_min_m") *value = g.opt.csr_device_min_m;
     else if (k == "wide_threads") *value = g.opt.wide_threads;
     else if (k == "debug_sched") *value = g.opt.debug_sched;
+    else if (k == "scratch_keep_mb") *value = g.opt.scratch_keep_mb;
     else return fail(FBC_ERR_INVALID_ARG, "unknown option " + k);
     return FBC_OK;
 }
@@ -1344,17 +1391,17 @@ int fbc_graph_from_text(const char* text, int64_t len, fbc_graph* out, fbc_stats
     if (st) std::memset(st, 0, sizeof(*st));
     const double t0 = now_ms();
     if (len > (int64_t)INT32_MAX - 2 * fbc::kTxTile) return fail(FBC_ERR_RANGE, "edge-list text longer than 2 GiB");
-    // the device copy ends in at least one space, so every token scan stops inside it
+    // the device copy ends in at least one space, so every token scan stops inside it, and has
+    // a halo of spaces past its last tile
     const int64_t ntiles = (len + 1 + fbc::kTxTile - 1) / fbc::kTxTile;
-    const size_t padded = (size_t)ntiles * fbc::kTxTile;
-    // capacities from the length alone (a token and its separator take two bytes, an edge six),
+    const size_t padded = (size_t)ntiles * fbc::kTxTile + fbc::kTxHalo;
+    // capacity from the length alone (a token and its separator take two bytes, a triple six),
     // so the passes run back to back with no host round trip
-    const int64_t tok_cap = (len + 1) / 2 + 1, edge_cap = (len + 1) / 6 + 1;
-    TmpBuf dtext, cnt, toff, tok, dsrc, ddst, dw, find, slow, fix_i, fix_v;
+    const int64_t edge_cap = (len + 1) / 6 + 1;
+    TmpBuf dtext, cnt, toff, dsrc, ddst, dw, find, slow, fix_i, fix_v;
     FBC_CK(dtext.ensure(padded));
     FBC_CK(cnt.ensure(sizeof(int32_t) * (size_t)ntiles));
     FBC_CK(toff.ensure(sizeof(int32_t) * ((size_t)ntiles + 1)));
-    FBC_CK(tok.ensure(sizeof(int32_t) * (size_t)tok_cap));
     FBC_CK(dsrc.ensure(sizeof(int32_t) * (size_t)edge_cap));
     FBC_CK(ddst.ensure(sizeof(int32_t) * (size_t)edge_cap));
     FBC_CK(dw.ensure(sizeof(double) * (size_t)edge_cap));
@@ -1369,16 +1416,14 @@ int fbc_graph_from_text(const char* text, int64_t len, fbc_graph* out, fbc_stats
     FBC_CK(cudaEventCreate(&ev[1]));
     cudaEventRecord(ev[0], g.st);
     const unsigned char* dt = (const unsigned char*)dtext.p;
-    const unsigned tgrid = (unsigned)std::min<int64_t>(ntiles, (int64_t)g.nsm * 8);
+    const unsigned tgrid = (unsigned)ntiles;  // one tile per block: many blocks in flight hide latency
     const int aux0 = g_aux_launches;
     fbc::tx_count_kernel<<<tgrid, fbc::kTxThreads, 0, g.st>>>(ntiles, dt, cnt.as<int32_t>());
     int rc = device_scan(cnt.as<int32_t>(), ntiles, toff.as<int32_t>());
-    if (rc == FBC_OK) {
-        fbc::tx_starts_kernel<<<tgrid, fbc::kTxThreads, 0, g.st>>>(ntiles, dt, toff.as<int32_t>(), tok.as<int32_t>());
-        fbc::tx_edges_kernel<<<grid_for(edge_cap), 256, 0, g.st>>>(toff.as<int32_t>() + ntiles, dt, tok.as<int32_t>(),
-                                                                  dsrc.as<int32_t>(), ddst.as<int32_t>(), dw.as<double>(),
+    if (rc == FBC_OK)
+        fbc::tx_tokens_kernel<<<tgrid, fbc::kTxThreads, 0, g.st>>>(ntiles, dt, toff.as<int32_t>(), dsrc.as<int32_t>(),
+                                                                  ddst.as<int32_t>(), dw.as<double>(),
                                                                   find.as<fbc::TxFind>(), slow.as<int2>());
-    }
     cudaEventRecord(ev[1], g.st);
     int32_t ntok = 0;
     cudaError_t ce = cudaGetLastError();
@@ -1394,7 +1439,7 @@ int fbc_graph_from_text(const char* text, int64_t len, fbc_graph* out, fbc_stats
     if (ce != cudaSuccess) return fail(FBC_ERR_CUDA, std::string("text parse: ") + cudaGetErrorString(ce));
     if (st) {
         st->kernel_ms = parse_ms;
-        st->launches = 2 + (g_aux_launches - aux0);  // count, starts, and the scan and edges kernels
+        st->launches = 2 + (g_aux_launches - aux0);  // count, tokens, and the scan's kernels
         st->h2d_bytes = len;
     }
     const int64_t nedges = ntok / 3;

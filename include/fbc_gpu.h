@@ -85,7 +85,9 @@ const char* fbc_last_error_string(void);
  * warp-per-source), "order_min_n" (batched runs relabel graphs of at least this many vertices
  * for memory locality, outputs in input ids), "iter_mult" (distance-pass rounds are capped at
  * iter_mult * (n + 2); 0 makes every unit stop at once with FBC_ERR_ITER_LIMIT, a host-side way to
- * exercise the bounded-loop error path), "ws_budget_mb".
+ * exercise the bounded-loop error path), "ws_budget_mb", "scratch_keep_mb" (per-call scratch
+ * -- graph builds, text parsing, class grouping -- comes from a stream-ordered memory pool that
+ * keeps up to this many MiB for later calls; default 8192).
  * Unknown key -> FBC_ERR_INVALID_ARG. */
 int fbc_set_option(const char* key, int64_t value);
 int fbc_get_option(const char* key, int64_t* value);
