@@ -529,7 +529,7 @@ def run_text_load(args):
             "e2e": {"value": el.m * args.steps / wall / 1e6, "unit": "M edges/s", "h2d_bytes_per_step": st.h2d_bytes,
                     "d2h_bytes_per_step": st.d2h_bytes},
             "parse_device_ms": parse_ms / args.steps, "gpu_launches": launches,
-            "roofline": {"bound": "hbm", "kernel": "tx_count + scan + tx_starts + tx_edges", "achieved": achieved,
+            "roofline": {"bound": "hbm", "kernel": "tx_count + scan + tx_tokens", "achieved": achieved,
                          "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_src,
                          "bytes_model": "text bytes + 16 per edge"},
             "clocks": ck}
