@@ -11,10 +11,12 @@
 #include <memory>
 #include <mutex>
 #include <numeric>
-#include <sstream>
 #include <string>
-#include <locale>
+#include <thread>
 #include <climits>
+#include <clocale>
+#include <cstdlib>
+#include <locale.h>
 #include <vector>
 
 #include "cluster_build.cuh"
@@ -1225,20 +1227,59 @@ int host_graph_from_edges(int64_t count, const int32_t* src, const int32_t* dst,
     return make_graph(n, std::move(rp), std::move(col), ww.data(), out);
 }
 
-// A weight token the device left to the host: operator>>(double&) of the classic locale on the
-// whole token, so overflow reads as the largest double with failbit set (the reference loop
-// then ends, DirectedWeightedGraph.h:83-86) and underflow as 0 or a subnormal.
+// A weight token the device left to the host, converted as operator>>(double&) does it in the
+// classic locale (libstdc++ hands the token to strtod there): overflow gives HUGE_VAL, which
+// operator>> turns into the largest double with failbit set, so the reference loop ends
+// (DirectedWeightedGraph.h:78-86); underflow gives 0 (rejected) or a subnormal.
 enum class TxHost { kValue, kStop, kNotPositive };
 TxHost tx_host_weight(const char* text, int64_t len, int64_t pos, double& v) {
+    static const locale_t c_locale = newlocale(LC_ALL_MASK, "C", (locale_t)0);
     int64_t end = pos;
     while (end < len && !(text[end] == ' ' || (text[end] >= 9 && text[end] <= 13))) ++end;
-    std::istringstream in(std::string(text + pos, (size_t)(end - pos)));
-    in.imbue(std::locale::classic());
-    v = 0.0;
-    in >> v;
+    char small[64];
+    std::string big;
+    const size_t n = (size_t)(end - pos);
+    char* buf = small;
+    if (n >= sizeof(small)) {
+        big.assign(text + pos, n);
+        buf = &big[0];
+    } else {
+        std::memcpy(small, text + pos, n);
+        small[n] = 0;
+    }
+    v = strtod_l(buf, nullptr, c_locale);
+    if (v == HUGE_VAL) return TxHost::kStop;
     if (!(v > 0)) return TxHost::kNotPositive;
-    if (in.fail()) return TxHost::kStop;
     return TxHost::kValue;
+}
+
+// The host conversions of a text, split over the host's cores when there are many.
+void tx_host_weights(const char* text, int64_t len, const std::vector<int2>& sl, std::vector<int32_t>& fi,
+                     std::vector<double>& fv, int64_t& stop, int64_t& bad_w) {
+    const size_t nt = sl.size() < 65536 ? 1 : std::max(1u, std::min(64u, std::thread::hardware_concurrency()));
+    std::vector<std::vector<int32_t>> ti(nt);
+    std::vector<std::vector<double>> tv(nt);
+    std::vector<int64_t> ts(nt, stop), tb(nt, bad_w);
+    auto work = [&](size_t k) {
+        for (size_t i = sl.size() * k / nt; i < sl.size() * (k + 1) / nt; ++i) {
+            double v = 0.0;
+            switch (tx_host_weight(text, len, sl[i].y, v)) {
+                case TxHost::kValue: ti[k].push_back(sl[i].x); tv[k].push_back(v); break;
+                case TxHost::kStop: ts[k] = std::min<int64_t>(ts[k], sl[i].x); break;
+                case TxHost::kNotPositive: tb[k] = std::min<int64_t>(tb[k], sl[i].x); break;
+            }
+        }
+    };
+    std::vector<std::thread> th;
+    for (size_t k = 1; k < nt; ++k) th.emplace_back(work, k);
+    work(0);
+    for (auto& t : th) t.join();
+    for (size_t k = 0; k < nt; ++k) {
+        fi.insert(fi.end(), ti[k].begin(), ti[k].end());
+        fv.insert(fv.end(), tv[k].begin(), tv[k].end());
+        stop = std::min(stop, ts[k]);
+        bad_w = std::min(bad_w, tb[k]);
+    }
 }
 
 }  // namespace
@@ -1451,14 +1492,7 @@ int fbc_graph_from_text(const char* text, int64_t len, fbc_graph* out, fbc_stats
         std::vector<int2> sl((size_t)hf.nslow);
         FBC_CK(cudaMemcpyAsync(sl.data(), slow.p, sizeof(int2) * sl.size(), cudaMemcpyDeviceToHost, g.st));
         FBC_CK(cudaStreamSynchronize(g.st));
-        for (const int2& t : sl) {
-            double v = 0.0;
-            switch (tx_host_weight(text, len, t.y, v)) {
-                case TxHost::kValue: fi.push_back(t.x); fv.push_back(v); break;
-                case TxHost::kStop: stop = std::min<int64_t>(stop, t.x); break;
-                case TxHost::kNotPositive: bad_w = std::min<int64_t>(bad_w, t.x); break;
-            }
-        }
+        tx_host_weights(text, len, sl, fi, fv, stop, bad_w);
     }
     // the first finding in text order decides (an id before the weight of its triple); nothing
     // after the end of reading counts

@@ -121,3 +121,23 @@ def test_from_file(fg, tmp_path):
     g = fg.Graph.from_file(str(p))
     assert _same(g.csr(), want)
     g.free()
+
+
+def test_many_host_converted_weights(fg):
+    # every weight past the device conversion (26 significant digits): the host converts them on
+    # several threads; an overflowing one late in the text still ends the reading there
+    rng = np.random.default_rng(8)
+    n, m = 5000, 150000
+    src = rng.integers(0, n, m)
+    src[:n] = np.arange(n)
+    dst = rng.integers(0, n, m)
+    w = rng.integers(1, 100, m)
+    lines = [b"%d %d %d.0000000000000000000000001\n" % (a, b, c) for a, b, c in zip(src, dst, w)]
+    text = b"".join(lines)
+    want = to.csr_from_edges_c(*to.parse_edge_text_c(text))
+    assert _same(_csr(fg, text), want)
+    cut = 140000
+    text2 = b"".join(lines[:cut] + [b"0 1 1" + b"0" * 400 + b"\n"] + lines[cut:])
+    want2 = to.csr_from_edges_c(*to.parse_edge_text_c(text2))
+    got2 = _csr(fg, text2)
+    assert _same(got2, want2) and int(got2[0][-1]) <= cut
