@@ -113,7 +113,7 @@ class GpuClusteredBrandesBC : public IBrandesBC<V, W> {
             for (const V& v : cl[i]->vertices()) cv.back().push_back((int32_t)v);
             for (const V& b : cl[i]->borders()) bv.back().push_back((int32_t)b);
         }
-        auto d = fbcgpu::DeviceGraph::from_graph(*graph, _o.device);
+        auto d = fbcgpu::device_graph_for(*graph, _o.device);
         // every cluster's all-sources Brandes in one call (ClusteredBrandesBC.h:91-110)
         std::vector<double> len;
         std::vector<uint64_t> cnt;

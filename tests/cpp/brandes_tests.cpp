@@ -36,6 +36,11 @@ struct MapGraph {
     }
     const std::vector<int>& vertices() const { return verts; }
     const std::map<int, double>& forwardStar(int v) const { return fs[v]; }
+    int edges() const {
+        int m = 0;
+        for (const auto& s : fs) m += (int)s.size();
+        return m;
+    }
 };
 
 // SubGraph stand-in: induced subgraph with border set (SubGraph.h:59-148).
@@ -56,6 +61,11 @@ struct MapSubGraph {
     }
     const std::vector<int>& vertices() const { return verts; }
     const std::map<int, double>& forwardStar(int v) const { return fs[v]; }
+    int edges() const {
+        int m = 0;
+        for (int v : verts) m += (int)fs[v].size();
+        return m;
+    }
     const std::set<int>& borders() const { return bord; }
     std::shared_ptr<const MapGraph> referenceGraph() const { return ref; }
 };
@@ -100,6 +110,33 @@ int main(int argc, char** argv) {
                                     1.6666666666666667, 1.3333333333333333, 0, 0, 0};
             for (int v = 0; v < 9; ++v) REQUIRE(std::fabs(dep[v] - want[v]) <= 1e-9 * std::fabs(want[v]));
         }
+    // the device graph parsed from the file stands for the host graph read from it: the same
+    // CSR as the upload of the host graph's stars, used by the engines given that host object
+    {
+        auto dg = fbcgpu::DeviceGraph::from_file(argc > 1 ? argv[1] : "DWGtext.txt");
+        auto up = fbcgpu::DeviceGraph::from_graph(*full);
+        std::vector<int64_t> rp1, rp2;
+        std::vector<int32_t> c1, c2;
+        std::vector<double> w1, w2;
+        dg->download_csr(rp1, c1, w1);
+        up->download_csr(rp2, c2, w2);
+        REQUIRE(rp1 == rp2 && c1 == c2 && w1 == w2);
+        fbcgpu::Options o;
+        auto before = fbcgpu::exact_bc<double>(*full, o);
+        fbcgpu::use_device_graph(full.get(), dg);
+        REQUIRE(fbcgpu::device_graph_for(*full, 0) == dg);
+        auto after = fbcgpu::exact_bc<double>(*full, o);
+        REQUIRE(before == after);
+        bool mismatch = false;  // a preload for an object with other counts is refused
+        fbcgpu::use_device_graph(&sub, dg);
+        try {
+            fbcgpu::exact_bc<double>(sub, o);
+        } catch (const fbcgpu::Error& e) {
+            mismatch = e.code == FBC_ERR_INVALID_ARG;
+        }
+        REQUIRE(mismatch);
+        fbcgpu::use_device_graph(nullptr, nullptr);
+    }
     // invalid input is reported as an exception carrying the library's status
     bool threw = false;
     try {
