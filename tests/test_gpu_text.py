@@ -141,3 +141,27 @@ def test_many_host_converted_weights(fg):
     want2 = to.csr_from_edges_c(*to.parse_edge_text_c(text2))
     got2 = _csr(fg, text2)
     assert _same(got2, want2) and int(got2[0][-1]) <= cut
+
+
+def test_dwg_text_constructor_getters(fg):
+    """DirectedWeightedGraph.cpp:11-40 (the reference's graph test) on DWGtext.txt parsed on the
+    device: 9 vertices, 16 edges, the forward and backward stars of vertex 4, edge weights."""
+    import os
+
+    from conftest import GOLDEN
+
+    g = fg.Graph.from_file(os.path.join(GOLDEN, "DWGtext.txt"))
+    assert (g.n, g.m) == (9, 16)
+    rp, col, w = g.csr()
+    g.free()
+    fs = dict(zip(col[rp[4]:rp[5]].tolist(), w[rp[4]:rp[5]].tolist()))
+    assert fs == {5: 1.0, 6: 5.0, 8: 3.0}
+    src = np.repeat(np.arange(9), np.diff(rp))
+    bs = {int(s): float(x) for s, d, x in zip(src, col, w) if d == 4}
+    assert bs == {0: 7.0, 2: 4.0, 3: 3.0}
+
+    def edge(a, b):
+        row = dict(zip(col[rp[a]:rp[a + 1]].tolist(), w[rp[a]:rp[a + 1]].tolist()))
+        return row.get(b, 0.0)
+
+    assert edge(7, 5) == 2 and edge(0, 1) == 4 and edge(1, 0) == 0
