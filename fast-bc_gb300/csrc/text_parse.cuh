@@ -205,6 +205,70 @@ __device__ __forceinline__ int tx_weight(const TxBytes& s, int32_t p, double& ou
     return 0;
 }
 
+// ---- fast path: whole tokens read eight bytes at a time from the staged tile ----
+
+// The 8 bytes at staged offset r, byte 0 first (r + 16 <= the staged length).
+__device__ __forceinline__ unsigned long long tx_load8(const unsigned char* sm, int r) {
+    const unsigned long long* wv = reinterpret_cast<const unsigned long long*>(sm + (r & ~7));
+    const unsigned sh = 8u * (unsigned)(r & 7);
+    const unsigned long long lo = wv[0], hi = wv[1];
+    return sh ? (lo >> sh) | (hi << (64u - sh)) : lo;
+}
+
+// bit i set where byte i of the 8 is a space
+__device__ __forceinline__ unsigned tx_space8(unsigned long long x) {
+    return tx_space4((unsigned)x) | (tx_space4((unsigned)(x >> 32)) << 4);
+}
+
+// The value of a token of len (1..8) bytes at the start of x when all of them are decimal digits,
+// else -1.  The digits are moved to the top of the word behind '0' bytes; a byte is a digit iff
+// adding 0x46 and subtracting 0x30 both leave its top bit clear; then pairs, quads and the two
+// halves are combined (10, 100, 10^4), each step staying inside its lane (99, 9999 and
+// 99,999,999 fit their 8, 16 and 32 bits).
+__device__ __forceinline__ long long tx_digits8(unsigned long long x, int len) {
+    const unsigned sh = 8u * (unsigned)(8 - len);
+    const unsigned long long z = 0x3030303030303030ull;
+    const unsigned long long t = sh ? (x << sh) | (z >> (64u - sh)) : x;
+    if (((t + 0x4646464646464646ull) | (t - z)) & 0x8080808080808080ull) return -1;
+    unsigned long long v = t - z;
+    v = ((v * 10u) + (v >> 8)) & 0x00FF00FF00FF00FFull;
+    v = ((v * 100u) + (v >> 16)) & 0x0000FFFF0000FFFFull;
+    v = ((v * 10000u) + (v >> 32)) & 0xFFFFFFFFull;
+    return (long long)v;
+}
+
+// A triple of plain decimal tokens of at most 8 digits each, separated by runs of fewer than 8
+// spaces, starting at staged offset r: its values (the weight > 0).  False when any of that does
+// not hold; the general path then reads the triple and reports what is wrong with it.
+__device__ __forceinline__ bool tx_triple_fast(const unsigned char* sm, int r, int lim, int32_t& a, int32_t& b,
+                                               double& x) {
+    long long val[3];
+#pragma unroll
+    for (int f = 0; f < 3; ++f) {
+        if (r + 16 > lim) return false;
+        unsigned long long w8 = tx_load8(sm, r);
+        unsigned sp = tx_space8(w8);
+        if (f > 0) {  // r is at the spaces after the previous token
+            const unsigned tok = ~sp & 0xffu;
+            if (!tok) return false;  // eight or more spaces
+            r += __ffs(tok) - 1;
+            if (r + 16 > lim) return false;
+            w8 = tx_load8(sm, r);
+            sp = tx_space8(w8);
+        }
+        if (!sp) return false;          // a token of more than 8 bytes
+        const int len = __ffs(sp) - 1;  // >= 1: r is at a token start
+        val[f] = tx_digits8(w8, len);
+        if (val[f] < 0) return false;   // a sign, point, exponent or other byte
+        r += len;
+    }
+    if (val[2] == 0) return false;  // a zero weight: the general path rejects it
+    a = (int32_t)val[0];
+    b = (int32_t)val[1];
+    x = (double)val[2];
+    return true;
+}
+
 // One tile per block iteration: token ranks from the scan (tile_off), the first-token offsets of
 // the triples starting in the tile gathered in shared memory, then one thread per triple.
 // Tokens past the last complete triple (text ending inside a triple) are left alone.
@@ -251,6 +315,13 @@ __global__ void __launch_bounds__(kTxThreads) tx_tokens_kernel(int64_t ntiles, c
         const TxBytes by{bytes, text, (int32_t)(t * kTxTile), kTxTile + kTxHalo};
         for (int32_t e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
             int32_t p = first[e - e0], a = 0, b = 0;
+            double xf = 0.0;
+            if (tx_triple_fast(bytes, p - by.base, by.lim, a, b, xf)) {
+                src[e] = a;
+                dst[e] = b;
+                w[e] = xf;
+                continue;
+            }
             bool oka, okb;
             p += tx_int(by, p, a, oka);
             p += tx_spaces(by, p);
