@@ -165,3 +165,23 @@ def test_dwg_text_constructor_getters(fg):
         return row.get(b, 0.0)
 
     assert edge(7, 5) == 2 and edge(0, 1) == 4 and edge(1, 0) == 0
+
+
+def test_long_ids_and_space_runs(fg):
+    # 7- and 8-digit ids (the eight-byte fast path takes tokens of at most 8 bytes with a space
+    # in view) and runs of 1..12 spaces or tabs between tokens, against the oracle
+    rng = np.random.default_rng(12)
+    n, m = 12_000_000, 60000
+    src = rng.integers(0, n, m)
+    dst = rng.integers(0, n, m)
+    src[0] = n - 1
+    w = rng.integers(1, 150, m)
+    seps = [b" " * k for k in range(1, 13)] + [b"\t" * k for k in (1, 7, 8, 9)]
+    parts = []
+    for i in range(m):
+        a = seps[rng.integers(len(seps))]
+        b = seps[rng.integers(len(seps))]
+        parts.append(b"%d%s%d%s%d\n" % (src[i], a, dst[i], b, w[i]))
+    text = b"".join(parts)
+    want = to.csr_from_edges_c(*to.parse_edge_text_c(text))
+    assert _same(_csr(fg, text), want)
