@@ -178,7 +178,10 @@ struct fbc_plan_s {
     std::vector<int32_t> cverts, borders;
     // frees everything the plan holds, also when its creation stopped half way
     ~fbc_plan_s() {
-        if (g.init) cudaStreamSynchronize(g.st);  // no launch in flight still uses a buffer
+        if (g.init) {  // no launch in flight still uses a buffer
+            cudaSetDevice(g.dev);
+            cudaStreamSynchronize(g.st);
+        }
         if (exec) cudaGraphExecDestroy(exec);
         if (graph) cudaGraphDestroy(graph);
         for (DBuf* b : {&crp, &cadj, &cgid, &cbord, &segs, &units, &chunks, &bc, &bdist, &bsig, &ctr, &retry})
@@ -192,8 +195,12 @@ struct fbc_plan_s {
 
 namespace {
 
+// Every entry point: the library is initialised, and the calling thread's current device is the
+// library's (OpenMP workers calling in start on device 0; allocations and launches must land on
+// the device of the library stream).
 int check_init() {
     if (!g.init) return fail(FBC_ERR_NOT_INIT, "fbc_gpu_init has not been called");
+    FBC_CK(cudaSetDevice(g.dev));
     return FBC_OK;
 }
 
@@ -1574,7 +1581,10 @@ int batched_graph_seg(fbc_graph_s* G, int64_t out_base, int sched, Seg& s, const
 int fbc_graph_free(fbc_graph G) {
     std::lock_guard<std::recursive_mutex> lk(g_mu);
     if (!G) return FBC_OK;
-    if (g.init) cudaStreamSynchronize(g.st);
+    if (g.init) {
+        cudaSetDevice(g.dev);
+        cudaStreamSynchronize(g.st);
+    }
     cudaFree(G->d_rp);
     cudaFree(G->d_adj);
     if (G->d_ord_rp) cudaFree(G->d_ord_rp);
