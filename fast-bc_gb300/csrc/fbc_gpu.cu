@@ -129,6 +129,21 @@ struct Ctx {
 };
 Ctx g;
 
+// Makes the library's device current for one entry point and gives the caller's back on return
+// (OpenMP workers calling in start on device 0, and allocations and launches must land on the
+// device of the library stream; a caller working on another device keeps it).
+struct DevGuard {
+    int prev = -1;
+    void enter() {
+        int cur = -1;
+        if (cudaGetDevice(&cur) == cudaSuccess && cur != g.dev && cudaSetDevice(g.dev) == cudaSuccess) prev = cur;
+    }
+    ~DevGuard() {
+        if (prev >= 0) cudaSetDevice(prev);
+    }
+};
+
+
 double now_ms() {
     return std::chrono::duration<double, std::milli>(
                std::chrono::steady_clock::now().time_since_epoch())
@@ -178,8 +193,9 @@ struct fbc_plan_s {
     std::vector<int32_t> cverts, borders;
     // frees everything the plan holds, also when its creation stopped half way
     ~fbc_plan_s() {
+        DevGuard dg_;
         if (g.init) {  // no launch in flight still uses a buffer
-            cudaSetDevice(g.dev);
+            dg_.enter();
             cudaStreamSynchronize(g.st);
         }
         if (exec) cudaGraphExecDestroy(exec);
@@ -195,12 +211,10 @@ struct fbc_plan_s {
 
 namespace {
 
-// Every entry point: the library is initialised, and the calling thread's current device is the
-// library's (OpenMP workers calling in start on device 0; allocations and launches must land on
-// the device of the library stream).
-int check_init() {
+// Every entry point: the library is initialised and its device is current.
+int check_init(DevGuard& dg) {
     if (!g.init) return fail(FBC_ERR_NOT_INIT, "fbc_gpu_init has not been called");
-    FBC_CK(cudaSetDevice(g.dev));
+    dg.enter();
     return FBC_OK;
 }
 
@@ -1406,7 +1420,8 @@ int fbc_get_option(const char* key, int64_t* value) {
 int fbc_graph_upload(int32_t n, const int64_t* row_ptr, const int32_t* col, const double* w,
                      fbc_graph* out) {
     std::lock_guard<std::recursive_mutex> lk(g_mu);
-    FBC_TRY(check_init());
+    DevGuard dg_;
+    FBC_TRY(check_init(dg_));
     if (!out || !row_ptr || n < 0) return fail(FBC_ERR_INVALID_ARG, "null argument");
     *out = nullptr;
     std::vector<int64_t> rp(row_ptr, row_ptr + (size_t)n + 1);
@@ -1420,7 +1435,8 @@ int fbc_graph_upload(int32_t n, const int64_t* row_ptr, const int32_t* col, cons
 int fbc_graph_from_edges(int64_t count, const int32_t* src, const int32_t* dst, const double* w,
                          fbc_graph* out) {
     std::lock_guard<std::recursive_mutex> lk(g_mu);
-    FBC_TRY(check_init());
+    DevGuard dg_;
+    FBC_TRY(check_init(dg_));
     if (!out || count < 0 || (count > 0 && (!src || !dst || !w)))
         return fail(FBC_ERR_INVALID_ARG, "null argument");
     *out = nullptr;
@@ -1433,7 +1449,8 @@ int fbc_graph_from_edges(int64_t count, const int32_t* src, const int32_t* dst, 
 
 int fbc_graph_from_text(const char* text, int64_t len, fbc_graph* out, fbc_stats* st) {
     std::lock_guard<std::recursive_mutex> lk(g_mu);
-    FBC_TRY(check_init());
+    DevGuard dg_;
+    FBC_TRY(check_init(dg_));
     if (!out || len < 0 || (len > 0 && !text)) return fail(FBC_ERR_INVALID_ARG, "null argument");
     *out = nullptr;
     if (st) std::memset(st, 0, sizeof(*st));
@@ -1554,7 +1571,8 @@ int fbc_graph_info(fbc_graph G, int32_t* n, int64_t* m) {
 int fbc_graph_download(fbc_graph G, int64_t* row_ptr, int32_t* col, double* w) {
     std::lock_guard<std::recursive_mutex> lk(g_mu);
     if (!G) return fail(FBC_ERR_INVALID_ARG, "null graph");
-    FBC_TRY(check_init());
+    DevGuard dg_;
+    FBC_TRY(check_init(dg_));
     FBC_TRY(ensure_host_csr(G));
     if (row_ptr) std::copy(G->h_rp.begin(), G->h_rp.end(), row_ptr);
     if (col) std::copy(G->h_col.begin(), G->h_col.end(), col);
@@ -1581,8 +1599,9 @@ int batched_graph_seg(fbc_graph_s* G, int64_t out_base, int sched, Seg& s, const
 int fbc_graph_free(fbc_graph G) {
     std::lock_guard<std::recursive_mutex> lk(g_mu);
     if (!G) return FBC_OK;
+    DevGuard dg_;
     if (g.init) {
-        cudaSetDevice(g.dev);
+        dg_.enter();
         cudaStreamSynchronize(g.st);
     }
     cudaFree(G->d_rp);
@@ -1596,7 +1615,8 @@ int fbc_graph_free(fbc_graph G) {
 
 int fbc_exact_bc(fbc_graph G, int precision, int sched, double* out_bc, fbc_stats* st) {
     std::lock_guard<std::recursive_mutex> lk(g_mu);
-    FBC_TRY(check_init());
+    DevGuard dg_;
+    FBC_TRY(check_init(dg_));
     if (!G || (!out_bc && G->n > 0)) return fail(FBC_ERR_INVALID_ARG, "null argument");
     FBC_TRY(check_sched(sched));
     const double t0 = now_ms();
@@ -1623,7 +1643,8 @@ int fbc_sssp_dependency_batch(fbc_graph G, int64_t count, const int32_t* sources
                               const double* cards, int precision, int sched, double* out_bc_accum,
                               fbc_stats* st) {
     std::lock_guard<std::recursive_mutex> lk(g_mu);
-    FBC_TRY(check_init());
+    DevGuard dg_;
+    FBC_TRY(check_init(dg_));
     if (!G || count < 0 || (count > 0 && !sources) || (!out_bc_accum && G->n > 0))
         return fail(FBC_ERR_INVALID_ARG, "null argument");
     FBC_TRY(check_sched(sched));
@@ -1653,7 +1674,8 @@ int fbc_sssp_dependency_batch(fbc_graph G, int64_t count, const int32_t* sources
 
 int fbc_single_source(fbc_graph G, int32_t source, int precision, double* out_dep, fbc_stats* st) {
     std::lock_guard<std::recursive_mutex> lk(g_mu);
-    FBC_TRY(check_init());
+    DevGuard dg_;
+    FBC_TRY(check_init(dg_));
     if (!G || !out_dep) return fail(FBC_ERR_INVALID_ARG, "null argument");
     std::fill(out_dep, out_dep + G->n, 0.0);
     const double one = 1.0;
@@ -1664,7 +1686,8 @@ int fbc_cluster_border_count(fbc_graph G, int32_t nclusters, const int64_t* coff
                              const int32_t* cverts, const int64_t* border_off, int64_t* out_nb,
                              int64_t* out_entries) {
     std::lock_guard<std::recursive_mutex> lk(g_mu);
-    FBC_TRY(check_init());
+    DevGuard dg_;
+    FBC_TRY(check_init(dg_));
     if (!G) return fail(FBC_ERR_INVALID_ARG, "null graph");
     std::vector<int64_t> boff;
     std::vector<int32_t> bl;
@@ -1689,7 +1712,8 @@ int fbc_cluster_border_count(fbc_graph G, int32_t nclusters, const int64_t* coff
 int fbc_cluster_borders(fbc_graph G, int32_t nclusters, const int64_t* coff, const int32_t* cverts,
                         int64_t* out_boff, int32_t* out_borders) {
     std::lock_guard<std::recursive_mutex> lk(g_mu);
-    FBC_TRY(check_init());
+    DevGuard dg_;
+    FBC_TRY(check_init(dg_));
     if (!G) return fail(FBC_ERR_INVALID_ARG, "null graph");
     std::vector<int64_t> boff;
     std::vector<int32_t> bl;
@@ -1705,7 +1729,8 @@ int fbc_cluster_classes(fbc_graph G, int32_t nclusters, const int64_t* coff, con
                         const double* bdist, const uint64_t* bsig, int64_t* out_class_off,
                         int32_t* out_pivots, int32_t* out_cards) {
     std::lock_guard<std::recursive_mutex> lk(g_mu);
-    FBC_TRY(check_init());
+    DevGuard dg_;
+    FBC_TRY(check_init(dg_));
     if (!G || !bc || !out_class_off || (border_off && !borders)) return fail(FBC_ERR_INVALID_ARG, "null argument");
     FBC_TRY(device_cluster_ids(G, nclusters, coff, cverts, nullptr));
     const int64_t nv = coff[nclusters];
@@ -1840,7 +1865,8 @@ int fbc_cluster_eval_batch(fbc_graph G, int32_t nclusters, const int64_t* coff,
                            int precision, int sched, double* out_intra_bc, double* out_bdist,
                            uint64_t* out_bsig, fbc_stats* st) {
     std::lock_guard<std::recursive_mutex> lk(g_mu);
-    FBC_TRY(check_init());
+    DevGuard dg_;
+    FBC_TRY(check_init(dg_));
     if (!G) return fail(FBC_ERR_INVALID_ARG, "null graph");
     FBC_TRY(check_sched(sched));
     if (border_off && !borders) return fail(FBC_ERR_INVALID_ARG, "border_off without borders");
@@ -1868,7 +1894,8 @@ int fbc_cluster_plan_create(fbc_graph G, int32_t nclusters, const int64_t* coff,
                             const int64_t* border_off, const int32_t* borders, int precision,
                             fbc_plan* out) {
     std::lock_guard<std::recursive_mutex> lk(g_mu);
-    FBC_TRY(check_init());
+    DevGuard dg_;
+    FBC_TRY(check_init(dg_));
     if (!G || !out || nclusters < 0 || !coff) return fail(FBC_ERR_INVALID_ARG, "null argument");
     if (precision != FBC_PREC_FP64 && precision != FBC_PREC_FP32C) return fail(FBC_ERR_INVALID_ARG, "unknown precision");
     *out = nullptr;
@@ -1965,7 +1992,8 @@ int fbc_cluster_plan_create(fbc_graph G, int32_t nclusters, const int64_t* coff,
 
 int fbc_plan_run(fbc_plan p, fbc_stats* st) {
     std::lock_guard<std::recursive_mutex> lk(g_mu);
-    FBC_TRY(check_init());
+    DevGuard dg_;
+    FBC_TRY(check_init(dg_));
     if (!p) return fail(FBC_ERR_INVALID_ARG, "null plan");
     const double t0 = now_ms();
     if (st) std::memset(st, 0, sizeof(*st));
@@ -2020,7 +2048,8 @@ int fbc_plan_free(fbc_plan p) {
 int fbc_multi_exact_bc(int32_t ngraphs, const fbc_graph* graphs, int precision, int sched,
                        double* const* out_bc, fbc_stats* st) {
     std::lock_guard<std::recursive_mutex> lk(g_mu);
-    FBC_TRY(check_init());
+    DevGuard dg_;
+    FBC_TRY(check_init(dg_));
     if (ngraphs < 0 || (ngraphs > 0 && (!graphs || !out_bc))) return fail(FBC_ERR_INVALID_ARG, "null argument");
     FBC_TRY(check_sched(sched));
     const double t0 = now_ms();
@@ -2054,7 +2083,8 @@ int fbc_multi_exact_bc(int32_t ngraphs, const fbc_graph* graphs, int precision, 
 int fbc_sssp_debug(fbc_graph G, int32_t source, int32_t* out_dist, uint64_t* out_sigma,
                    double* out_delta, int32_t* out_npred) {
     std::lock_guard<std::recursive_mutex> lk(g_mu);
-    FBC_TRY(check_init());
+    DevGuard dg_;
+    FBC_TRY(check_init(dg_));
     if (!G || source < 0 || source >= G->n) return fail(FBC_ERR_INVALID_ARG, "bad graph or source");
     const size_t n = (size_t)G->n;
     FBC_CK(g.dbg.ensure(n * (4 + 8 + 8) + 512));
