@@ -31,7 +31,7 @@ def _rank(rank, world, port, out):
 
 def test_two_rank_max_and_value():
     port = _free_port()
-    with mp.Manager() as m:
+    with mp.get_context("spawn").Manager() as m:  # no fork of this (threaded) process
         out = m.dict()
         mp.spawn(_rank, args=(2, port, out), nprocs=2, join=True)
         res = dict(out)
