@@ -5,7 +5,7 @@
 // ("Edge weight must be greater than zero"), and reading ends at the end of the text.
 //
 // Two passes over the bytes, each thread loading 64 of them as four 16-byte loads:
-//   tx_count  -- token starts per 4 KiB tile (a non-space byte after a space byte or the start);
+//   tx_count  -- token starts per 16 KiB tile (a non-space byte after a space byte or the start);
 //   (a scan of the tile counts gives every token its index k in the text)
 //   tx_tokens -- the block of a tile lists the triples whose first token (index k = 3e) starts
 //                in it, then one thread per triple parses its three tokens (so the threads of a
