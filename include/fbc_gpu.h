@@ -7,7 +7,7 @@
  *   ISSBrandesBC<V,W>::singleSourceBrandes    libfastbc/include/brandes/ISSBrandesBC.h:26-28
  *   IClusterEvaluator<V,W>::evaluateCluster   libfastbc/include/brandes/IClusterEvaluator.h:33-36
  * Each entry point below is what an implementation of one of those interfaces calls
- * (include/fastbc_gpu/*.hpp hold the C++ classes that implement them on top of this ABI).
+ * (the headers under include/fastbc_gpu hold the C++ classes that implement them on top of this ABI).
  * Plain pointers and sizes only; every call returns FBC_OK or an FBC_ERR_* status and
  * never throws; fbc_last_error_string() describes the last failure of the calling thread.
  * Calls are serialised by an internal mutex, so OpenMP worker threads may call in

@@ -37,3 +37,22 @@ def test_calls_fail_cleanly_before_init():
     rc = lib.fbc_graph_upload(1, rp, None, None, C.byref(out))
     assert rc in (7, 2)  # FBC_ERR_NOT_INIT (or a CUDA error where no driver is present)
     assert lib.fbc_last_error_string()
+
+
+def test_header_is_plain_c(tmp_path):
+    """A C program (no C++) includes the header without warnings and links every entry point."""
+    import shutil
+    import subprocess
+
+    import pytest
+
+    gcc = shutil.which("gcc")
+    if not gcc:
+        pytest.skip("gcc not available")
+    calls = "\n".join(f"    (void)&{n};" for n in declared())
+    src = tmp_path / "abi.c"
+    src.write_text('#include "fbc_gpu.h"\nint main(void) {\n' + calls + "\n    return 0;\n}\n")
+    r = subprocess.run([gcc, "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror", "-I",
+                        os.path.join(ROOT, "include"), str(src), "-L", os.path.dirname(LIB), "-lfbcgpu",
+                        "-o", str(tmp_path / "abi")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-2000:]
