@@ -433,3 +433,11 @@ def clustered_bc(g: Graph, cs: ClusterSet, pivots: list, cards: list, precision:
     if stats is not None:
         stats.extend([st1, st2])
     return bc
+
+
+def write_bc(path: str, bc) -> None:
+    """The fbc CLI's result file (main.cpp:123-130, 282-294): one value per line as an ostream
+    prints a double (six significant digits, the %g form), entries that are not >= 0 written
+    as 0; an existing file is refused (FileExistsError), as the CLI refuses it."""
+    with open(path, "x") as f:
+        f.write("".join(("%g\n" % x) if x >= 0 else "0\n" for x in np.asarray(bc, np.float64).tolist()))

@@ -244,4 +244,17 @@ inline void dependency_batch(const DeviceGraph& d, const std::vector<int32_t>& p
                                     o.precision, o.sched, acc.data(), nullptr));
 }
 
+// The fbc CLI's result file (main.cpp:123-130, 282-294): one value per line as the stream
+// prints it, values that are not >= 0 written as 0; an existing file is refused.
+template <class W>
+void write_bc(const std::string& path, const std::vector<W>& bc) {
+    if (std::ifstream(path).good()) throw Error(FBC_ERR_INVALID_ARG, "File \"" + path + "\" already existing");
+    std::ofstream out(path);
+    for (const W& x : bc) {
+        if (x >= 0) out << x << '\n';
+        else out << 0 << '\n';
+    }
+    if (!out) throw Error(FBC_ERR_INVALID_ARG, "cannot write " + path);
+}
+
 }  // namespace fbcgpu
