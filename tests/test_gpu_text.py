@@ -84,6 +84,8 @@ def test_empty_and_blank_texts(fg):
     for text in (b"", b" \n\t\r\n  "):
         g = fg.Graph.from_text(text)
         assert (g.n, g.m) == (0, 0)
+        for sched in (fg.PLAIN, fg.BATCHED):
+            assert fg.exact_bc(g, fg.FP64, sched).size == 0
         g.free()
 
 
