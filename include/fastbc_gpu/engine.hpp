@@ -74,6 +74,16 @@ class DeviceGraph {
         return d;
     }
 
+    // n vertices and no edges.
+    static std::shared_ptr<DeviceGraph> edgeless(int64_t n, int device = 0) {
+        ensure_device(device);
+        std::vector<int64_t> rp((size_t)n + 1, 0);
+        auto d = std::make_shared<DeviceGraph>();
+        check(fbc_graph_upload((int32_t)n, rp.data(), nullptr, nullptr, &d->h_));
+        d->n_ = (int32_t)n;
+        return d;
+    }
+
     // From the bytes of an edge-list file (the format fbc reads), parsed on the device.
     static std::shared_ptr<DeviceGraph> from_text(const std::string& text, int device = 0) {
         ensure_device(device);
@@ -242,6 +252,76 @@ inline void dependency_batch(const DeviceGraph& d, const std::vector<int32_t>& p
                              std::vector<double>& acc) {
     check(fbc_sssp_dependency_batch(d.handle(), (int64_t)pivots.size(), pivots.data(), cards.data(),
                                     o.precision, o.sched, acc.data(), nullptr));
+}
+
+// An edgeless device graph of n vertices: the id range the class grouping checks cluster lists
+// against when no graph is at hand (one per n, kept for the process).
+inline fbc_graph id_range_graph(int64_t n, int device) {
+    static std::mutex mu;
+    static std::map<int64_t, std::shared_ptr<DeviceGraph>> cache;
+    std::lock_guard<std::mutex> lk(mu);
+    auto& d = cache[n];
+    if (!d) d = DeviceGraph::edgeless(n, device);
+    return d->handle();
+}
+
+// VertexInfoPivotSelector::selectPivots (VertexInfoPivotSelector.h:30-123) for one cluster with
+// the class grouping on the device (fbc_cluster_classes).  Applies when every cluster vertex's
+// info holds one entry per border of `borders` and the borders are cluster vertices -- the
+// clustered pipeline's case (use_device_classes tells); returns (pivots, cardinalities) in
+// class order.  As the reference's loop does, each cluster vertex's info is normalized in place
+// (the k-means step that may follow reads them so).  A class made only of borders gives its
+// first member as pivot when pivot_border is true (FASTBC_BRANDES_ENABLE_PIVOT_BORDER), else no
+// pivot.  VIPtr: a pointer to an object with normalize(), borders(), getBorderSPLength(j),
+// getBorderSPCount(j).
+template <class V, class VIPtr>
+bool use_device_classes(const std::vector<VIPtr>& vi, const std::vector<V>& vertices, const std::set<V>& borders) {
+    std::set<V> members(vertices.begin(), vertices.end());
+    if (members.size() != vertices.size()) return false;
+    for (const V& b : borders)
+        if (!members.count(b)) return false;
+    for (const V& v : vertices)
+        if (v < 0 || (size_t)v >= vi.size() || !vi[v] || (size_t)vi[v]->borders() != borders.size()) return false;
+    return true;
+}
+
+template <class V, class W, class VIPtr>
+std::pair<std::vector<V>, std::vector<V>> select_pivots(const std::vector<W>& bc, const std::vector<VIPtr>& vi,
+                                                        const std::vector<V>& vertices, const std::set<V>& borders,
+                                                        bool pivot_border, int device = 0) {
+    const size_t nc = vertices.size(), nb = borders.size();
+    std::pair<std::vector<V>, std::vector<V>> out;
+    if (nc == 0) return out;
+    std::vector<double> bd(nc * nb);
+    std::vector<uint64_t> bs(nc * nb);
+    for (size_t i = 0; i < nc; ++i) {
+        const auto& p = vi[vertices[i]];
+        p->normalize();
+        for (size_t j = 0; j < nb; ++j) {
+            bd[i * nb + j] = (double)p->getBorderSPLength((int)j);
+            bs[i * nb + j] = (uint64_t)(int64_t)p->getBorderSPCount((int)j);
+        }
+    }
+    if (nb == 0) {  // every (empty) vector is equal: one class, its least-BC member (first on ties)
+        V best = vertices[0];
+        for (const V& v : vertices)
+            if (bc[v] < bc[best]) best = v;
+        out.first.push_back(best);
+        out.second.push_back((V)nc);
+        return out;
+    }
+    std::vector<int64_t> coff{0, (int64_t)nc}, boff{0, (int64_t)nb}, class_off(2);
+    std::vector<int32_t> cv(vertices.begin(), vertices.end()), bv(borders.begin(), borders.end());
+    std::vector<double> bcd(bc.begin(), bc.end());
+    std::vector<int32_t> piv(nc), card(nc);
+    check(fbc_cluster_classes(id_range_graph((int64_t)bc.size(), device), 1, coff.data(), cv.data(), boff.data(),
+                              bv.data(), bcd.data(), bd.data(), bs.data(), class_off.data(), piv.data(), card.data()));
+    for (int64_t k = 0; k < class_off[1]; ++k) {
+        if (!pivot_border && borders.count((V)piv[k])) continue;  // a class of borders only
+        out.first.push_back((V)piv[k]);
+        out.second.push_back((V)card[k]);
+    }
+    return out;
 }
 
 // The fbc CLI's result file (main.cpp:123-130, 282-294): one value per line as the stream

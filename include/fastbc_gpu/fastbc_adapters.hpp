@@ -8,6 +8,12 @@
 //   GpuSSBrandesBC          : ISSBrandesBC       replaces DijkstraSSBrandesBC (DijkstraSSBrandesBC.h:45-81)
 //   GpuClusterEvaluator     : IClusterEvaluator  replaces DijkstraClusterEvaluator
 //                                                (DijkstraClusterEvaluator.h:50-180)
+//   GpuVertexInfoPivotSelector : IPivotSelector  replaces VertexInfoPivotSelector
+//                                                (VertexInfoPivotSelector.h:30-123): the exact
+//                                                topological classes grouped on the device (the
+//                                                reference's own selector for inputs outside the
+//                                                clustered pipeline's shape); usable as the
+//                                                exact selector inside KMeansPivotSelector
 //   GpuClusteredBrandesBC   : IBrandesBC         ClusteredBrandeBC (ClusteredBrandesBC.h:63-169)
 //                             with one GPU call for all clusters and one for all pivots; the
 //                             partition and pivot selection are the caller's reference objects.
@@ -84,6 +90,31 @@ class GpuClusterEvaluator : public IClusterEvaluator<V, W> {
     fbcgpu::Options _o;
     fbcgpu::GraphCache _cache;
     std::mutex _out_mu;
+};
+
+template <typename V, typename W>
+class GpuVertexInfoPivotSelector : public IPivotSelector<V, W> {
+  public:
+    explicit GpuVertexInfoPivotSelector(fbcgpu::Options o = {}) : _o(o) {}
+    std::pair<std::vector<V>, std::vector<V>> selectPivots(const std::vector<W>& globalBC,
+                                                           const std::vector<std::shared_ptr<VertexInfo<V, W>>>& verticesInfo,
+                                                           const std::vector<V>& vertices,
+                                                           const std::set<V>& borders) override {
+        if (!fbcgpu::use_device_classes(verticesInfo, vertices, borders))
+            return _host.selectPivots(globalBC, verticesInfo, vertices, borders);
+#ifdef FASTBC_BRANDES_ENABLE_PIVOT_BORDER
+        const bool pivot_border = true;
+#else
+        const bool pivot_border = false;
+#endif
+        std::lock_guard<std::mutex> lk(_mu);  // pivot selection may run on OpenMP workers
+        return fbcgpu::select_pivots<V, W>(globalBC, verticesInfo, vertices, borders, pivot_border, _o.device);
+    }
+
+  private:
+    fbcgpu::Options _o;
+    VertexInfoPivotSelector<V, W> _host;
+    std::mutex _mu;
 };
 
 template <typename V, typename W>

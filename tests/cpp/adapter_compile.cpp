@@ -40,6 +40,12 @@ int main(int argc, char** argv) {
         gp, std::make_shared<GpuClusterEvaluator<V, W>>(o), std::make_shared<GpuSSBrandesBC<V, W>>(o), ps);
     // batched GPU orchestration
     std::shared_ptr<IBrandesBC<V, W>> batched = std::make_shared<GpuClusteredBrandesBC<V, W>>(gp, ps, o);
+    // the exact class grouping on the device inside the reference's k-means selector
+    std::shared_ptr<IPivotSelector<V, W>> gps = std::make_shared<KMeansPivotSelector<V, W>>(
+        std::make_shared<GpuVertexInfoPivotSelector<V, W>>(o),
+        std::shared_ptr<kmeans::IKMeans<V, W>>(new kmeans::PlusPlusKMeans<V, W>()), 0.5);
+    std::shared_ptr<IBrandesBC<V, W>> batched_gps = std::make_shared<GpuClusteredBrandesBC<V, W>>(gp, gps, o);
+    (void)batched_gps;
     if (argc > 2) {
         std::string mode = argv[2];
         std::vector<W> bc = mode == "exact" ? exact->computeBC(graph)

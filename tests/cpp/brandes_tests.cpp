@@ -2,6 +2,7 @@
 // GPU engines of include/fastbc_gpu/engine.hpp.  The graph types here are small test
 // doubles with the reference's IGraph/ISubGraph surface (vertices, forwardStar, borders,
 // referenceGraph); the fixture is the reference's DWGtext.txt.
+#include <algorithm>
 #include <fastbc_gpu/engine.hpp>
 
 #include <cmath>
@@ -70,6 +71,22 @@ struct MapSubGraph {
     std::shared_ptr<const MapGraph> referenceGraph() const { return ref; }
 };
 
+// VertexInfo stand-in (VertexInfo.h): border path lengths (W) and counts (V); normalize subtracts
+// the least length (VertexInfo.h:259-278).
+struct MiniVI {
+    std::vector<double> len;
+    std::vector<int> cnt;
+    MiniVI(std::vector<double> l, std::vector<int> c) : len(std::move(l)), cnt(std::move(c)) {}
+    int borders() const { return (int)len.size(); }
+    double getBorderSPLength(int j) const { return len[j]; }
+    int getBorderSPCount(int j) const { return cnt[j]; }
+    void normalize() {
+        if (len.empty()) return;
+        const double m = *std::min_element(len.begin(), len.end());
+        for (double& x : len) x -= m;
+    }
+};
+
 int main(int argc, char** argv) {
     std::ifstream f(argc > 1 ? argv[1] : "DWGtext.txt");
     auto full = std::make_shared<MapGraph>(f);
@@ -136,6 +153,37 @@ int main(int argc, char** argv) {
         }
         REQUIRE(mismatch);
         fbcgpu::use_device_graph(nullptr, nullptr);
+    }
+    // "Pivot selection" (VertexInfoPivotSelector.cpp:14-74) with the class grouping on the device:
+    // that test's global BC and the first two border entries of its vertex infos, borders {0, 4}.
+    // Normalized: v0 (0,1 | 2,1), v1 (1,0 | 2,2), v2 (0,1 | 2,1), v3 (1,0 | 2,2), v4 (4,0 | 1,1):
+    // classes {0,2}, {1,3}, {4}; pivots the least-BC non-border member (2; 3 with BC 1.5 < 2),
+    // and for the all-border class {4} its first member, or none.
+    {
+        std::vector<double> gbc{1, 2, 2, 1.5, 1, 3};
+        auto make = [] {
+            std::vector<std::shared_ptr<MiniVI>> vi;
+            vi.push_back(std::make_shared<MiniVI>(std::vector<double>{1, 2}, std::vector<int>{2, 1}));
+            vi.push_back(std::make_shared<MiniVI>(std::vector<double>{2, 1}, std::vector<int>{2, 2}));
+            vi.push_back(std::make_shared<MiniVI>(std::vector<double>{2, 3}, std::vector<int>{2, 1}));
+            vi.push_back(std::make_shared<MiniVI>(std::vector<double>{4, 3}, std::vector<int>{2, 2}));
+            vi.push_back(std::make_shared<MiniVI>(std::vector<double>{5, 1}, std::vector<int>{1, 1}));
+            vi.push_back(nullptr);
+            return vi;
+        };
+        std::vector<int> verts{0, 1, 2, 3, 4};
+        std::set<int> bord{0, 4};
+        auto vi = make();
+        REQUIRE(fbcgpu::use_device_classes(vi, verts, bord));
+        auto p = fbcgpu::select_pivots<int, double>(gbc, vi, verts, bord, true);
+        REQUIRE((p.first == std::vector<int>{2, 3, 4}) && (p.second == std::vector<int>{2, 2, 1}));
+        REQUIRE(vi[3]->len[0] == 1.0 && vi[3]->len[1] == 0.0);  // normalized in place, as the reference does
+        vi = make();
+        p = fbcgpu::select_pivots<int, double>(gbc, vi, verts, bord, false);
+        REQUIRE((p.first == std::vector<int>{2, 3}) && (p.second == std::vector<int>{2, 2}));
+        // outside the pipeline's shape (the reference test's empty border set with 3-entry infos):
+        // the device path does not apply
+        REQUIRE(!fbcgpu::use_device_classes(vi, verts, std::set<int>{}));
     }
     // invalid input is reported as an exception carrying the library's status
     bool threw = false;
