@@ -62,3 +62,16 @@ def test_c_oracle_matches_python_oracle():
             except to.TextError as e:
                 outs.append((e.kind, e.edge))
         assert outs[0] == outs[1], text
+
+
+def test_edge_list_text_formatter():
+    """graphs.EdgeList.text() (array formatting of the bench's text workload) writes exactly the
+    "src dst w" lines a plain formatter writes, and the text oracle reads them back."""
+    import graphs
+
+    for el in (graphs.road_grid(48, 40, seed=3), graphs.rgg_knn(3000, seed=2)):
+        want = b"".join(b"%d %d %d\n" % (a, b, c) for a, b, c in zip(el.src, el.dst, el.w))
+        text = el.text()
+        assert text == want
+        s, d, w = to.parse_edge_text_c(text)
+        assert np.array_equal(s, el.src) and np.array_equal(d, el.dst) and np.array_equal(w, el.w)
