@@ -79,15 +79,25 @@ int fbc_gpu_init(int device);
 int fbc_gpu_shutdown(void);
 const char* fbc_last_error_string(void);
 
-/* Tuning knobs (the autotuner sets these): "delta" bucket width (0 = automatic),
- * "block_threads", "frontier_threads", "group" (sources per block of the frontier kernel:
- * 1, 2, 4, or 0 = automatic), "chunk_max", "wide_n", "warp_max_n" (largest segment run
- * warp-per-source), "order_min_n" (batched runs relabel graphs of at least this many vertices
- * for memory locality, outputs in input ids), "iter_mult" (distance-pass rounds are capped at
- * iter_mult * (n + 2); 0 makes every unit stop at once with FBC_ERR_ITER_LIMIT, a host-side way to
- * exercise the bounded-loop error path), "ws_budget_mb", "scratch_keep_mb" (per-call scratch
- * -- graph builds, text parsing, class grouping -- comes from a stream-ordered memory pool that
- * keeps up to this many MiB for later calls; default 8192).
+/* Tuning knobs (the autotuner sets the first ones); values outside a knob's range are clamped:
+ *   "delta"            bucket width of the distance pass (0 = 4 x the graph's mean weight)
+ *   "block_threads"    block size of the plain kernel (32..1024)
+ *   "frontier_threads" block size of the frontier kernel (32..128; above 128 the wide form)
+ *   "group"            sources per frontier block: 1, 2, 4, or 0 = automatic (others refused)
+ *   "chunk_max"        sources per work item of the shared-memory kernel
+ *   "wide_n"           segments of at least this many vertices use the wide frontier blocks
+ *   "wide_threads"     block size of the wide frontier blocks (64..512, a multiple of 32)
+ *   "warp_max_n"       largest segment run warp-per-source in shared memory
+ *   "order_min_n"      batched runs relabel graphs of at least this many vertices for memory
+ *                      locality (outputs stay in input ids)
+ *   "csr_device_min_m" edge lists of at least this many edges are built into a CSR on the device
+ *   "iter_mult"        distance-pass rounds are capped at iter_mult * (n + 2); 0 makes every unit
+ *                      stop at once with FBC_ERR_ITER_LIMIT (a host-side way to exercise the
+ *                      bounded-loop error path)
+ *   "ws_budget_mb"     cap of the block kernels' workspace (0 = 60% of the free device memory)
+ *   "debug_sched"      schedule of fbc_sssp_debug (0 plain, else batched)
+ *   "scratch_keep_mb"  per-call scratch (graph builds, text parsing, class grouping) comes from a
+ *                      stream-ordered memory pool that keeps up to this many MiB (default 8192)
  * Unknown key -> FBC_ERR_INVALID_ARG. */
 int fbc_set_option(const char* key, int64_t value);
 int fbc_get_option(const char* key, int64_t* value);

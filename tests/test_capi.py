@@ -56,3 +56,45 @@ def test_header_is_plain_c(tmp_path):
                         os.path.join(ROOT, "include"), str(src), "-L", os.path.dirname(LIB), "-lfbcgpu",
                         "-o", str(tmp_path / "abi")], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-2000:]
+
+
+OPTIONS = ["delta", "block_threads", "frontier_threads", "group", "chunk_max", "wide_n", "warp_max_n",
+           "order_min_n", "iter_mult", "ws_budget_mb", "csr_device_min_m", "wide_threads", "debug_sched",
+           "scratch_keep_mb"]
+
+
+def test_options_round_trip_and_limits():
+    """The tuning knobs (host state, no GPU needed): every key the header documents reads back
+    what was set within its documented range, out-of-range values are clamped, a bad group or an
+    unknown key is refused with FBC_ERR_INVALID_ARG."""
+    lib = C.CDLL(LIB)
+    lib.fbc_set_option.argtypes = [C.c_char_p, C.c_int64]
+    lib.fbc_get_option.argtypes = [C.c_char_p, C.POINTER(C.c_int64)]
+    src = open(HEADER).read()
+    for k in OPTIONS:
+        assert f'"{k}"' in src, k
+    saved = {}
+    for k in OPTIONS:
+        v = C.c_int64()
+        assert lib.fbc_get_option(k.encode(), C.byref(v)) == 0
+        saved[k] = v.value
+
+    def get(k):
+        v = C.c_int64()
+        assert lib.fbc_get_option(k.encode(), C.byref(v)) == 0
+        return v.value
+
+    try:
+        for k, v in [("delta", 37), ("chunk_max", 64), ("group", 2), ("order_min_n", 0), ("iter_mult", 3)]:
+            assert lib.fbc_set_option(k.encode(), v) == 0 and get(k) == v
+        assert lib.fbc_set_option(b"block_threads", 5000) == 0 and get("block_threads") == 1024
+        assert lib.fbc_set_option(b"frontier_threads", 1) == 0 and get("frontier_threads") == 32
+        assert lib.fbc_set_option(b"wide_threads", 300) == 0 and get("wide_threads") == 288
+        assert lib.fbc_set_option(b"delta", -5) == 0 and get("delta") == 0
+        assert lib.fbc_set_option(b"group", 3) == 1
+        assert lib.fbc_set_option(b"no_such_knob", 1) == 1
+        v = C.c_int64()
+        assert lib.fbc_get_option(b"no_such_knob", C.byref(v)) == 1
+    finally:
+        for k, v in saved.items():
+            lib.fbc_set_option(k.encode(), v)
