@@ -98,6 +98,7 @@ def _load():
         f = getattr(lib, name)
         f.argtypes = args
         f.restype = res
+    lib.signatures = sig
     return lib
 
 

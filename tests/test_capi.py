@@ -98,3 +98,20 @@ def test_options_round_trip_and_limits():
     finally:
         for k, v in saved.items():
             lib.fbc_set_option(k.encode(), v)
+
+
+def test_every_entry_point_refuses_cleanly_before_init():
+    """Each entry point called before fbc_gpu_init with zero sizes and null pointers returns a
+    status (FBC_ERR_NOT_INIT, or FBC_ERR_INVALID_ARG where the arguments are checked first; OK for
+    the no-op frees) instead of dereferencing anything (CPU: the library never initialises here)."""
+    import fastbc_gpu as fg
+
+    skip = {"fbc_gpu_init", "fbc_last_error_string", "fbc_set_option", "fbc_get_option"}
+    for name, (args, res) in sorted(fg.lib.signatures.items()):
+        if name in skip:
+            continue
+        vals = [None if a in (C.c_void_p, C.c_char_p) or hasattr(a, "contents") else 0 for a in args]
+        rc = getattr(fg.lib, name)(*vals)
+        assert rc in (0, fg.FBC_ERR_INVALID_ARG, fg.FBC_ERR_NOT_INIT), (name, rc)
+        if name in ("fbc_graph_free", "fbc_plan_free", "fbc_gpu_shutdown"):
+            assert rc == 0, name
