@@ -15,6 +15,8 @@ oracle/_ref/ref_harness) single-threaded on the seeded workloads and stores:
                              2048x2048 grid: community id per vertex (int16; every
                              community's vertices are ascending, as the reference lists them)
   DWGtext.txt                the reference unit tests' 9-vertex fixture (copied)
+  rgg1500_exact_bc.txt       ExactBrandesBC<int,double> over a 1,500-point random geometric graph
+                             (3-NN, weights ceil(1000 d): the family of the 48-graph batch)
   text/<case>.txt, .out      edge-list texts in the formats operator>> accepts (layout, number
                              forms, weights past a double's fast conversion, overflow ending the
                              reading, rejected weights) and what DirectedWeightedGraph(istream&)
@@ -23,6 +25,7 @@ The clustered run takes about 15 minutes on one core, the 2048x2048 partition ab
 minute on eight.  Usage:
   python tests/golden/make_golden.py [--reuse DIR]   (DIR: outputs of an earlier harness run)
   python tests/golden/make_golden.py --only text     (the text/ fixtures alone, seconds)
+  python tests/golden/make_golden.py --only rgg      (the random-geometric-graph golden, seconds)
 """
 from __future__ import annotations
 
@@ -109,6 +112,13 @@ def text_cases() -> dict:
     return cases
 
 
+def rgg_golden() -> None:
+    work = tempfile.mkdtemp()
+    p = os.path.join(work, "rgg1500.txt")
+    graphs.rgg_knn(1500, seed=11).write(p)
+    run("exact", p, os.path.join(HERE, "rgg1500_exact_bc.txt"))
+
+
 def text_goldens() -> None:
     tdir = os.path.join(HERE, "text")
     os.makedirs(tdir, exist_ok=True)
@@ -122,11 +132,14 @@ def text_goldens() -> None:
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reuse", default=None)
-    ap.add_argument("--only", choices=["text"], default=None)
+    ap.add_argument("--only", choices=["text", "rgg"], default=None)
     a = ap.parse_args()
     subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref", f"REF={REF}"], check=True)
-    text_goldens()
-    if a.only == "text":
+    if a.only != "rgg":
+        text_goldens()
+    if a.only != "text":
+        rgg_golden()
+    if a.only:
         return
     shutil.copy(os.path.join(REF, "libfastbc", "test", "DWGtext.txt"), os.path.join(HERE, "DWGtext.txt"))
     work = a.reuse or tempfile.mkdtemp()

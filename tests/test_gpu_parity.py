@@ -142,9 +142,15 @@ def test_grid256_pivot_batch(fg, prec):
 
 
 def test_rgg_small_exact(fg):
+    """The oracle's exact BC here equals the reference's bit for bit (tests/golden/
+    rgg1500_exact_bc.txt, pinned in tests/test_oracle.py)."""
+    import os
+    from conftest import GOLDEN
+
     el = graphs.rgg_knn(1500, seed=11)
     og = oracle.CSR.from_edgelist(el)
     ref = oracle.exact_bc(og)
+    assert np.array_equal(ref, np.loadtxt(os.path.join(GOLDEN, "rgg1500_exact_bc.txt")))
     g = fg.Graph.from_edgelist(el)
     for prec, tol in ((fg.FP64, TOL_FP64), (fg.FP32C, TOL_FP32C)):
         for sched in (fg.PLAIN, fg.BATCHED):

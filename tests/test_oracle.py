@@ -107,3 +107,11 @@ def test_generators_are_stable():
     assert int(el.w.sum()) == 12506652
     assert graphs.WORKLOADS["grid32"]().m == 3968
     assert graphs.rgg_sizes()[:3] == [1765, 2433, 1422]
+
+
+def test_rgg_exact_matches_reference_bitwise():
+    """A 1,500-point random geometric graph (3-NN, weights ceil(1000 d); the 48-graph batch's
+    family): the oracle's exact BC equals the reference's, bit for bit."""
+    golden = np.loadtxt(os.path.join(GOLDEN, "rgg1500_exact_bc.txt"))
+    bc = oracle.exact_bc(oracle.CSR.from_edgelist(graphs.rgg_knn(1500, seed=11)))
+    assert np.array_equal(bc, golden)
