@@ -17,6 +17,7 @@ oracle/_ref/ref_harness) single-threaded on the seeded workloads and stores:
   DWGtext.txt                the reference unit tests' 9-vertex fixture (copied)
   rgg1500_exact_bc.txt       ExactBrandesBC<int,double> over a 1,500-point random geometric graph
                              (3-NN, weights ceil(1000 d): the family of the 48-graph batch)
+  rgg1500_ss.npz             DijkstraSSBrandesBC dependency vectors on it for three sources
   text/<case>.txt, .out      edge-list texts in the formats operator>> accepts (layout, number
                              forms, weights past a double's fast conversion, overflow ending the
                              reading, rejected weights) and what DirectedWeightedGraph(istream&)
@@ -117,6 +118,13 @@ def rgg_golden() -> None:
     p = os.path.join(work, "rgg1500.txt")
     graphs.rgg_knn(1500, seed=11).write(p)
     run("exact", p, os.path.join(HERE, "rgg1500_exact_bc.txt"))
+    srcs = [0, 700, 1499]
+    deps = []
+    for s in srcs:
+        o = os.path.join(work, f"ss{s}.txt")
+        run("ss", p, s, o)
+        deps.append(np.loadtxt(o))
+    np.savez_compressed(os.path.join(HERE, "rgg1500_ss.npz"), sources=np.array(srcs), dep=np.array(deps))
 
 
 def text_goldens() -> None:

@@ -115,3 +115,11 @@ def test_rgg_exact_matches_reference_bitwise():
     golden = np.loadtxt(os.path.join(GOLDEN, "rgg1500_exact_bc.txt"))
     bc = oracle.exact_bc(oracle.CSR.from_edgelist(graphs.rgg_knn(1500, seed=11)))
     assert np.array_equal(bc, golden)
+
+
+def test_rgg_single_source_matches_reference_bitwise():
+    """DijkstraSSBrandesBC::singleSourceBrandes on the same graph for three sources."""
+    z = np.load(os.path.join(GOLDEN, "rgg1500_ss.npz"))
+    g = oracle.CSR.from_edgelist(graphs.rgg_knn(1500, seed=11))
+    for s, dep in zip(z["sources"], z["dep"]):
+        assert np.array_equal(oracle.single_source(g, int(s)), dep)
