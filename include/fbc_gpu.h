@@ -12,7 +12,8 @@
  * never throws; fbc_last_error_string() describes the last failure of the calling thread.
  * Calls are serialised by an internal mutex, so OpenMP worker threads may call in
  * concurrently (the reference calls singleSourceBrandes from OMP workers,
- * ClusteredBrandesBC.h:143-148).
+ * ClusteredBrandesBC.h:143-148).  Each call makes the device given to fbc_gpu_init current for
+ * its duration and gives the calling thread its own current device back on return.
  *
  * Graphs: directed, positive integer weights (the README's input contract), vertex ids
  * 0..n-1, each CSR row sorted ascending without repeats (the std::map order of
