@@ -682,6 +682,11 @@ def main():
     prev = {"ev": fg.ClusterEval(pinned(np.zeros(g.n)), pinned(np.zeros(ent)), pinned(np.zeros(ent, np.uint64)),
                                  cs, entry_off)}
     bcbuf = pinned(np.zeros(g.n))
+    # per vertex: the summed pivot cardinalities of its cluster (ClusteredBrandesBC.h:158-164
+    # subtracts intraBC[v] * card once per pivot of v's cluster); 0 outside evaluated clusters
+    mult = np.zeros(g.n)
+    for c in range(len(clusters)):
+        mult[clusters[c]] = float(np.sum(cards[keep[c]]))
 
     def step():
         st1, st2 = fg.Stats(), fg.Stats()
@@ -690,10 +695,7 @@ def main():
         knobs("pivots")
         bcbuf[:] = ev.intra_bc
         bc = fg.dependency_batch(g, allp, allc, prec, sched, out=bcbuf, stats=st2)
-        for c in range(len(clusters)):
-            tot = float(np.sum(cards[keep[c]]))
-            if tot:
-                bc[clusters[c]] -= ev.intra_bc[clusters[c]] * tot
+        bc -= ev.intra_bc * mult  # BC[v] -= intraBC[v] * (cards of v's cluster) in one pass
         return bc, st1, st2
 
     for _ in range(max(args.warmup, 0)):

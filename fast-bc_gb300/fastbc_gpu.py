@@ -426,11 +426,12 @@ def clustered_bc(g: Graph, cs: ClusterSet, pivots: list, cards: list, precision:
     allp = np.concatenate([np.asarray(p, np.int32) for p in pivots]) if pivots else np.zeros(0, np.int32)
     allc = np.concatenate([np.asarray(c, np.float64) for c in cards]) if cards else np.zeros(0)
     dependency_batch(g, allp, allc, precision, sched, out=bc, stats=st2)
-    for c in range(cs.count):
-        tot = float(np.sum(np.asarray(cards[c], np.float64))) if len(cards[c]) else 0.0
-        if tot:
-            vs = cs.vertices[cs.off[c]:cs.off[c + 1]]
-            bc[vs] -= ev.intra_bc[vs] * tot
+    # BC[v] -= intraBC[v] * (summed cardinalities of v's cluster's pivots), all clusters at once
+    tot = np.array([float(np.sum(np.asarray(cards[c], np.float64))) if len(cards[c]) else 0.0
+                    for c in range(cs.count)])
+    mult = np.zeros(g.n)
+    mult[cs.vertices] = np.repeat(tot, np.diff(cs.off))
+    bc -= ev.intra_bc * mult
     if stats is not None:
         stats.extend([st1, st2])
     return bc
