@@ -18,6 +18,8 @@ oracle/_ref/ref_harness) single-threaded on the seeded workloads and stores:
   rgg1500_exact_bc.txt       ExactBrandesBC<int,double> over a 1,500-point random geometric graph
                              (3-NN, weights ceil(1000 d): the family of the 48-graph batch)
   rgg1500_ss.npz             DijkstraSSBrandesBC dependency vectors on it for three sources
+  rgg1500_cluster.npz        DijkstraClusterEvaluator on its cluster of ids 0..499: intra BC,
+                             borders, border lengths and counts
   text/<case>.txt, .out      edge-list texts in the formats operator>> accepts (layout, number
                              forms, weights past a double's fast conversion, overflow ending the
                              reading, rejected weights) and what DirectedWeightedGraph(istream&)
@@ -125,6 +127,22 @@ def rgg_golden() -> None:
         run("ss", p, s, o)
         deps.append(np.loadtxt(o))
     np.savez_compressed(os.path.join(HERE, "rgg1500_ss.npz"), sources=np.array(srcs), dep=np.array(deps))
+    # DijkstraClusterEvaluator on the cluster of ids 0..499 (spatially scattered: most members
+    # are borders, and many borders are unreachable from a member)
+    vf = os.path.join(work, "verts.txt")
+    with open(vf, "w") as f:
+        f.write(" ".join(str(v) for v in range(500)))
+    pre = os.path.join(work, "clu")
+    run("cluster", p, vf, pre)
+    bc = np.loadtxt(pre + ".bc")
+    with open(pre + ".vi") as f:
+        lines = f.read().split("\n")
+    nb = int(lines[0])
+    borders = np.array(lines[1].split(), np.int32) if nb else np.zeros(0, np.int32)
+    vals = [np.array(lines[2 + i].split(), np.float64).reshape(nb, 2) if nb else np.zeros((0, 2))
+            for i in range(500)]
+    np.savez_compressed(os.path.join(HERE, "rgg1500_cluster.npz"), intra_bc=bc, borders=borders,
+                        border_len=np.array([v[:, 0] for v in vals]), border_cnt=np.array([v[:, 1] for v in vals]))
 
 
 def text_goldens() -> None:

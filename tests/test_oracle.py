@@ -123,3 +123,13 @@ def test_rgg_single_source_matches_reference_bitwise():
     g = oracle.CSR.from_edgelist(graphs.rgg_knn(1500, seed=11))
     for s, dep in zip(z["sources"], z["dep"]):
         assert np.array_equal(oracle.single_source(g, int(s)), dep)
+
+
+def test_rgg_cluster_matches_reference_bitwise():
+    """DijkstraClusterEvaluator on a scattered cluster of the same graph (489 of its 500 members
+    are borders, many unreachable from a member): intra BC and every border (length, count)."""
+    z = np.load(os.path.join(GOLDEN, "rgg1500_cluster.npz"))
+    g = oracle.CSR.from_edgelist(graphs.rgg_knn(1500, seed=11))
+    bc, bd, bs = oracle.cluster_eval(g, np.arange(500, dtype=np.int32), z["borders"])
+    assert np.array_equal(bc, z["intra_bc"])
+    assert np.array_equal(bd, z["border_len"]) and np.array_equal(bs, z["border_cnt"])
