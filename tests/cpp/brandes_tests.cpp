@@ -105,7 +105,7 @@ int main(int argc, char** argv) {
             REQUIRE(bc[2] == 0.5f);
             REQUIRE(bc[3] == 1.0f);
             REQUIRE(bc[4] == 0.0f);
-            // "Dijkstra cluster evaluation test" (DijkstraClusterEvaluator.cpp:15-109)
+            // "Dijkstra cluster evaluation test" (DijkstraClusterEvaluator.cpp:15-74)
             auto d = fbcgpu::DeviceGraph::from_graph(*full);
             std::vector<std::vector<int32_t>> cv{{0, 1, 2, 3, 4}}, bv{{3, 4}};
             std::vector<double> len;

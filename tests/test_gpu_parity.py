@@ -84,7 +84,7 @@ def test_dwg_exact_bc_matches_reference_golden(fg):
 
 
 def test_dwg_subgraph_known_answers(fg):
-    """ExactBrandesBC.cpp:31-35 and DijkstraClusterEvaluator.cpp:73-109 on SubGraph {0..4}."""
+    """ExactBrandesBC.cpp:31-35 and DijkstraClusterEvaluator.cpp:38-74 on SubGraph {0..4}."""
     s, d, w = dwg()
     g = fg.Graph.from_edges(s, d, w)
     cs = fg.ClusterSet.from_lists([[0, 1, 2, 3, 4]])

@@ -39,7 +39,7 @@ def test_exact_subgraph_known_answer():
 
 
 def test_cluster_evaluator_known_answers():
-    """libfastbc/test/brandes/DijkstraClusterEvaluator.cpp:73-109."""
+    """libfastbc/test/brandes/DijkstraClusterEvaluator.cpp:38-74."""
     g = dwg_csr()
     bc, bd, bs = oracle.cluster_eval(g, [0, 1, 2, 3, 4], [3, 4])
     assert list(bc) == [2, 2, 0.5, 1, 0, 0, 0, 0, 0]
