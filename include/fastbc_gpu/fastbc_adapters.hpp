@@ -128,7 +128,7 @@ class GpuClusteredBrandesBC : public IBrandesBC<V, W> {
         const size_t n = graph->vertices().size();
         std::vector<W> globalBC(n, (W)0);
         std::vector<std::shared_ptr<VertexInfo<V, W>>> vi(n, nullptr);
-        // Louvain on the host, as in the reference (ClusteredBrandesBC.h:81-82)
+        // Louvain on the host, as in the reference (ClusteredBrandesBC.h:80-81)
         auto communities = _gp->partitionGraph(std::static_pointer_cast<const IDegreeGraph<V, W>>(graph));
         std::vector<std::shared_ptr<ISubGraph<V, W>>> cl(communities.size());
         std::vector<size_t> evaluated;

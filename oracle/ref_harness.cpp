@@ -134,7 +134,7 @@ int main(int argc, char** argv) {
         return 0;
     }
     if (mode == "partition" && argc == 6) {
-        // LouvainGraphPartition::partitionGraph alone (ClusteredBrandesBC.h:75-76): one line per
+        // LouvainGraphPartition::partitionGraph alone (ClusteredBrandesBC.h:80-81): one line per
         // community, its vertices in the reference's order.
         auto g = load(argv[2]);
         std::set<std::mt19937::result_type> seeds;
