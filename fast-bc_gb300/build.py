@@ -13,9 +13,8 @@ ROOT = os.path.dirname(HERE)
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = [os.path.join(HERE, "csrc", "fbc_gpu.cu"), os.path.join(HERE, "csrc", "noalloc.cu")]
-HEADERS = [os.path.join(HERE, "csrc", f) for f in
-           ("brandes_kernels.cuh", "batched_kernels.cuh", "frontier_kernels.cuh")] + \
-          [os.path.join(ROOT, "include", "fbc_gpu.h")]
+HEADERS = sorted(os.path.join(HERE, "csrc", f) for f in os.listdir(os.path.join(HERE, "csrc"))
+                 if f.endswith(".cuh")) + [os.path.join(ROOT, "include", "fbc_gpu.h")]
 OUT = os.path.join(HERE, "libfbcgpu.so")
 
 
