@@ -19,6 +19,7 @@ def _digest(el):
     ("grid32", 1024, 3968, "ac21d0068a03fda3"),
     ("grid256", 65536, 248528, "513ac0956aea3b3c"),
     ("grid512", 262144, 995164, "9d895bd3c3a0e9b3"),
+    ("grid2048", 4194304, 15937326, "3e54ba2f8bfe20f6"),  # the partition golden's graph (~10 s)
 ])
 def test_road_grids(name, n, m, digest):
     el = graphs.WORKLOADS[name]()
