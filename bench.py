@@ -601,7 +601,8 @@ def main():
     ap.add_argument("--no-autotune", action="store_true",
                     help="batched schedule: keep the default knobs instead of tuning them first")
     ap.add_argument("--small", action="store_true",
-                    help="profiling case: 8 clusters and 256 pivots of the same workload")
+                    help="profiling case: 8 clusters and 256 pivots of the same workload "
+                         "(text-load: the 512x512 grid's text)")
     ap.add_argument("--max-pivots", type=int, default=0,
                     help="grid2048-clustered: at most this many pivots per step (profiling cases)")
     ap.add_argument("--no-precision", action="store_true",
