@@ -215,18 +215,23 @@ int fbc_sssp_debug(fbc_graph g, int32_t source, int32_t* out_dist, uint64_t* out
  * block-per-source kernel for callers that cannot allocate device memory -- code inside a
  * framework's memory pool or a custom allocator that owns every device byte, or a library
  * handed device buffers and a stream by its host application.  It allocates nothing: the
- * graph (d_row_ptr: n+1 int32 row offsets; d_adj: 2*m int32, (destination, weight) pairs,
- * weights > 0) and the output (d_dep: n doubles, overwritten, d_dep[source] = 0) are the
- * caller's device buffers, the work runs on the caller's stream (NULL: the default stream),
- * and the per-source work area is a fixed device array inside the library, sized for
- * FBC_NOALLOC_MAX_N vertices (about 12.6 MB, held by every GPU that loads the library until
- * the process exits).  Larger n is rejected with FBC_ERR_RANGE.  fbc_gpu_init is not needed.
+ * graph (d_row_ptr: n+1 int32 row offsets, row_ptr[0] = 0 and row_ptr[n] = m; d_adj: 2*m int32,
+ * (destination, weight) pairs, each row's destinations strictly ascending, weights > 0) and the
+ * output (d_dep: n doubles, overwritten, d_dep[source] = 0) are the caller's device buffers, the
+ * work runs on the caller's stream (NULL: the default stream), and the per-source work area is a
+ * fixed device array inside the library, sized for FBC_NOALLOC_MAX_N vertices (about 12.6 MB,
+ * held by every GPU that loads the library until the process exits).  Larger n is rejected with
+ * FBC_ERR_RANGE; a malformed CSR (checked on the device, reading only row_ptr[0..n] and
+ * d_adj[0..2m)) with FBC_ERR_INVALID_ARG.  fbc_gpu_init is not needed.
  * The first call on a device looks up that array's device address (once per device, with the
- * device current): make that first call before any stream capture.  All calls share the one
- * array, so calls whose work overlaps on the GPU (other streams, other host threads) race and
- * must be serialised by the caller.  Results equal fbc_single_source's. */
+ * device current).  Every call ends by reading its status back with a synchronisation of the
+ * caller's stream, so the entry point cannot be called while that stream is being captured.
+ * All calls share the one array, so calls whose work overlaps on the GPU (other streams, other
+ * host threads) race and must be serialised by the caller.  A source whose path counts pass
+ * 2^64 - 1 is run again with FP64 counts, as fbc_single_source does; results agree with
+ * fbc_single_source's within the precision form's tolerance. */
 #define FBC_NOALLOC_MAX_N 262144
-int fbc_single_source_noalloc(int32_t n, const int32_t* d_row_ptr, const int32_t* d_adj,
+int fbc_single_source_noalloc(int32_t n, int64_t m, const int32_t* d_row_ptr, const int32_t* d_adj,
                               int32_t source, int precision, double* d_dep, void* stream);
 
 #ifdef __cplusplus
