@@ -759,13 +759,11 @@ def main():
         with open(peaks_path) as f:
             peak, peak_src = float(json.load(f)["hbm_gbs"]), "measured"
     traffic = None
-    ceiling = None
     tpath = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tpath):
         with open(tpath) as f:
             tj = json.load(f)
         traffic = tj.get(f"{dom}_{args.prec}_{args.sched}")
-        ceiling = tj.get("random_access_ceiling_gsectors")
     line = {"metric": METRIC, "value": value, "unit": "GTEPS", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": tot_dev / args.steps * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -787,14 +785,6 @@ def main():
                          "peak_source": peak_src,
                          "bytes_model": "40*m + 52*n per (segment, source) unit"},
             "clocks": clk}
-    if traffic and ceiling and kern[f"{dom}_ms"]:
-        # the same kernel against the device's random-access ceiling: its DRAM traffic per launch
-        # (ncu) in 32-byte sectors over its per-launch event time
-        per_launch_ms = kern[f"{dom}_ms"] / args.steps
-        achieved_s = traffic / 32.0 / (per_launch_ms / 1e3) / 1e9
-        line["random_access_roofline"] = {"achieved": achieved_s, "peak": ceiling, "unit": "G sectors/s",
-                                          "frac": achieved_s / ceiling, "kernel": dom,
-                                          "peak_source": "measured (random_access_probe, 512 threads/SM, multi-GB footprint)"}
     if not args.no_cpu_baseline:
         v, dt, what = cpu_sample(el, z, os.cpu_count() or 1)
         line["cpu_baseline"] = {"value": v, "unit": "GTEPS", "cores": os.cpu_count() or 1, "kind": "port",

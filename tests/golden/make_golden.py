@@ -43,7 +43,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
-REF = "/root/reference"
+REF = os.environ.get("FASTBC_REF_DIR", "")  # the reference checkout; required
 HARNESS = os.path.join(ROOT, "oracle", "_ref", "ref_harness")
 sys.path.insert(0, os.path.join(ROOT, "fast-bc_gb300"))
 import graphs  # noqa: E402
@@ -160,6 +160,8 @@ def main():
     ap.add_argument("--reuse", default=None)
     ap.add_argument("--only", choices=["text", "rgg"], default=None)
     a = ap.parse_args()
+    if not REF or not os.path.isdir(os.path.join(REF, "libfastbc")):
+        sys.exit("set FASTBC_REF_DIR to the reference checkout")
     subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref", f"REF={REF}"], check=True)
     if a.only != "rgg":
         text_goldens()

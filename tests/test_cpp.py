@@ -15,7 +15,7 @@ import pytest
 
 from conftest import GOLDEN, ROOT
 
-REF = "/root/reference"
+REF = os.environ.get("FASTBC_REF_DIR", "")  # the reference checkout (unset: skipped)
 LIBDIR = os.path.join(ROOT, "fast-bc_gb300")
 
 
