@@ -137,8 +137,12 @@ struct PrecF64 {
     // ExactBrandesBC.h:81: sigma[v] / sigma[w] * (1.0 + delta[w]), division first
     // path counts arrive as doubles: exact below 2^53, where the reference's double counts
     // are exact too
-    __device__ static void add(Acc& a, double sv, double sw, D dw) {
+    __device__ static void add_d(Acc& a, double sv, double sw, D dw) {
         a.s += sv / sw * (1.0 + dw);
+    }
+    // uint64 counts (exact below 2^53 as doubles, rounded as the reference's double sums)
+    __device__ static void add(Acc& a, unsigned long long sv, unsigned long long sw, D dw) {
+        add_d(a, (double)sv, (double)sw, dw);
     }
     // sigma_v == sigma_w: the ratio is exactly 1.0 and 1.0 * y == y
     __device__ static void add_same(Acc& a, D dw) { a.s += 1.0 + dw; }
@@ -162,18 +166,36 @@ struct PrecDF32 {
         s = __fadd_rn(a, b);
         e = __fsub_rn(b, __fsub_rn(s, a));
     }
-    __device__ static void add(Acc& a, double sv, double sw, D dw) {
-        // ratio r = sv / sw as a double-float
+    // ratio r = x / y of two counts up to 2^24 (exact in FP32) as a double-float
+    __device__ static void ratio32(float x, float y, float& rh, float& rl) {
+        rh = __fdiv_rn(x, y);
+        rl = __fdiv_rn(__fmaf_rn(-rh, y, x), y);  // the remainder x - rh*y is exact
+    }
+    // counts above 2^24: the ratio in FP64, split into a double-float
+    __device__ static void ratio64(double sv, double sw, float& rh, float& rl) {
+        const double rd = sv / sw;
+        rh = __double2float_rn(rd);
+        rl = __double2float_rn(rd - (double)rh);
+    }
+    // uint64 counts: compared with 2^24 and converted to FP32 as integers, so a ratio of small
+    // counts (every ratio on road-like graphs) touches no FP64 instruction
+    __device__ static void add(Acc& a, unsigned long long sv, unsigned long long sw, D dw) {
         float rh, rl;
-        if (sv <= 16777216.0 && sw <= 16777216.0) {
-            float x = (float)sv, y = (float)sw;   // exact
-            rh = __fdiv_rn(x, y);
-            rl = __fdiv_rn(__fmaf_rn(-rh, y, x), y);  // the remainder x - rh*y is exact
-        } else {
-            double rd = sv / sw;  // FP64 only above 2^24
-            rh = __double2float_rn(rd);
-            rl = __double2float_rn(rd - (double)rh);
-        }
+        if (sv <= 16777216ull && sw <= 16777216ull)
+            ratio32(__uint2float_rn((unsigned)sv), __uint2float_rn((unsigned)sw), rh, rl);
+        else
+            ratio64((double)sv, (double)sw, rh, rl);
+        mul_add(a, rh, rl, dw);
+    }
+    // FP64 counts (the plain kernel's rerun of units whose uint64 counts overflowed)
+    __device__ static void add_d(Acc& a, double sv, double sw, D dw) {
+        float rh, rl;
+        if (sv <= 16777216.0 && sw <= 16777216.0) ratio32((float)sv, (float)sw, rh, rl);
+        else ratio64(sv, sw, rh, rl);
+        mul_add(a, rh, rl, dw);
+    }
+    // acc += (rh, rl) * (1 + dw)
+    __device__ static void mul_add(Acc& a, float rh, float rl, D dw) {
         // t = 1 + delta_w
         float s, e, th, tl;
         two_sum(1.0f, dw.x, s, e);
@@ -566,15 +588,16 @@ __device__ void run_unit(const KParams& P, const Unit& u, const State<Prec>& S, 
             for (int i = a0 + G::rank(); i < a1; i += G::size()) {
                 const int v = order[i];
                 const int dv = ld_i32<kSh>(S.dist + v);
-                const double sv = sig_val<kSigF64>(ld_u64<kSh>(S.sig + v));
+                const unsigned long long bv = ld_u64<kSh>(S.sig + v);  // raw count bits
                 typename Prec::Acc acc = Prec::zero();
                 const int e1 = rp[v + 1];
                 for (int e = rp[v]; e < e1; ++e) {
                     const int2 a = __ldg(adj + e);
                     if (dv + a.y == ld_i32<kSh>(S.dist + a.x)) {
-                        const double sx = sig_val<kSigF64>(ld_u64<kSh>(S.sig + a.x));
-                        if (sx == sv) Prec::add_same(acc, S.dlt[a.x]);
-                        else Prec::add(acc, sv, sx, S.dlt[a.x]);
+                        const unsigned long long bx = ld_u64<kSh>(S.sig + a.x);
+                        if (bx == bv) Prec::add_same(acc, S.dlt[a.x]);
+                        else if constexpr (kSigF64) Prec::add_d(acc, sig_val<true>(bv), sig_val<true>(bx), S.dlt[a.x]);
+                        else Prec::add(acc, bv, bx, S.dlt[a.x]);
                     }
                 }
                 S.dlt[v] = Prec::store(acc);

@@ -332,6 +332,31 @@ def test_rgg_batch_smallest_graphs(fg):
                 assert rel_err(o, oracle.exact_bc(oracle.CSR.from_edgelist(e))) <= tol
 
 
+def test_rgg_batch_all_graphs(fg):
+    """The whole 48-graph batch (n from 1,128 to 58,453) in one persistent launch, as the batching
+    bench runs it: the 24 smallest graphs' exact BC against the oracle's (FP64 1e-9, FP32C 1e-6),
+    every graph's FP32C result within 1e-6 of its FP64 one, and on every one of the 48 graphs a
+    seeded sample of 6 sources through the batched kernels against the oracle."""
+    import os
+
+    threads = os.cpu_count() or 1
+    els = graphs.rgg_batch(48)
+    gs = [fg.Graph.from_edgelist(e) for e in els]
+    f64 = fg.multi_exact_bc(gs, fg.FP64, fg.BATCHED)
+    f32 = fg.multi_exact_bc(gs, fg.FP32C, fg.BATCHED)
+    by_size = sorted(range(len(els)), key=lambda i: els[i].n)
+    for i in by_size[:24]:
+        ref = oracle.exact_bc(oracle.CSR.from_edgelist(els[i]), threads=threads)
+        assert rel_err(f64[i], ref) <= TOL_FP64, f"graph {i} (n={els[i].n})"
+        assert rel_err(f32[i], ref) <= TOL_FP32C, f"graph {i} (n={els[i].n})"
+    for i, e in enumerate(els):
+        assert rel_err(f32[i], f64[i]) <= TOL_FP32C, f"graph {i} (n={e.n})"
+        src = np.unique(graphs.rand_int(31, i, np.arange(6), 0, e.n - 1)).astype(np.int32)
+        ref = oracle.exact_bc_sources(oracle.CSR.from_edgelist(e), src, threads=threads)
+        got = fg.dependency_batch(gs[i], src, None, fg.FP64, fg.BATCHED)
+        assert rel_err(got, ref) <= TOL_FP64, f"graph {i} (n={e.n})"
+
+
 def test_grid512_precision_form(fg):
     """Precision configuration (512x512 grid): on 512 sampled sources the FP32-compensated form
     stays within 1e-6 of the FP64 form (itself within 1e-9 of the oracle on a subset), and
