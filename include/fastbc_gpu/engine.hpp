@@ -324,6 +324,82 @@ std::pair<std::vector<V>, std::vector<V>> select_pivots(const std::vector<W>& bc
     return out;
 }
 
+// ClusteredBrandeBC::computeBC (ClusteredBrandesBC.h:63-169) with one device call for every
+// cluster's all-sources Brandes and one for every pivot.  The parts the reference keeps on the
+// host are the caller's callables, so the adapter passes the reference's own objects and a test
+// passes stand-ins:
+//   partition(graph)                    -> std::vector<std::vector<V>>  (ClusteredBrandesBC.h:80-81)
+//   make_cluster(community)             -> a pointer to an ISubGraph-like object (vertices(),
+//                                          borders() as std::set<V>)       (SubGraph.h:59-148)
+//   make_info(nb)                       -> a pointer to a VertexInfo-like object with
+//                                          setBorderSPLength(int, W), setBorderSPCount(int, V)
+//   select(bc, infos, vertices, borders)-> (pivots, cardinalities)        (IPivotSelector.h)
+// Order of the reference kept: clusters without borders skipped when ignore_unconnected
+// (FASTBC_BRANDES_CLUSTERED_IGNORE_UNCONNECTED), evaluated otherwise (they then get no pivot
+// from a selector that needs borders); each cluster's vertex infos hold the unreached-border
+// length 0 and the count converted W -> V as DijkstraClusterEvaluator.h:166-177 stores it; pivot
+// selection per cluster in cluster order after every evaluation -- the same selection as the
+// reference's evaluate-then-select per cluster, because a cluster's evaluation writes only its
+// own vertices' BC and infos and its selection reads only those; the pivot sum and the
+// per-pivot subtraction of intraBC * cardinality (ClusteredBrandesBC.h:141-166).
+template <class V, class W, class G, class Partition, class MakeCluster, class MakeInfo, class Select>
+std::vector<W> clustered_bc(const G& graph, Partition&& partition, MakeCluster&& make_cluster,
+                            MakeInfo&& make_info, Select&& select, const Options& o,
+                            bool ignore_unconnected, std::shared_ptr<DeviceGraph> dev = nullptr) {
+    const size_t n = graph.vertices().size();
+    std::vector<W> globalBC(n, (W)0);
+    using Info = decltype(make_info(0));
+    std::vector<Info> vi(n, nullptr);
+    std::vector<std::vector<V>> communities = partition(graph);
+    using Cluster = decltype(make_cluster(communities[0]));
+    std::vector<Cluster> cl(communities.size());
+    std::vector<size_t> evaluated;
+    std::vector<std::vector<int32_t>> cv, bv;
+    for (size_t i = 0; i < cl.size(); ++i) {
+        cl[i] = make_cluster(communities[i]);
+        if (ignore_unconnected && cl[i]->borders().empty()) continue;
+        evaluated.push_back(i);
+        cv.emplace_back();
+        bv.emplace_back();
+        for (const V& v : cl[i]->vertices()) cv.back().push_back((int32_t)v);
+        for (const V& b : cl[i]->borders()) bv.back().push_back((int32_t)b);
+    }
+    auto d = dev ? dev : device_graph_for(graph, o.device);
+    std::vector<double> len;
+    std::vector<uint64_t> cnt;
+    std::vector<int64_t> eo;
+    std::vector<double> intra = cluster_eval_batch(*d, cv, bv, o, &len, &cnt, &eo);
+    for (size_t k = 0; k < evaluated.size(); ++k) {
+        const size_t nb = bv[k].size();
+        for (size_t i = 0; i < cv[k].size(); ++i) {
+            const int32_t v = cv[k][i];
+            globalBC[v] += (W)intra[v];
+            vi[v] = make_info((int)nb);
+            for (size_t j = 0; j < nb; ++j) {
+                vi[v]->setBorderSPLength((int)j, (W)len[eo[k] + i * nb + j]);
+                vi[v]->setBorderSPCount((int)j, (V)(W)cnt[eo[k] + i * nb + j]);
+            }
+        }
+    }
+    std::vector<std::pair<std::vector<V>, std::vector<V>>> piv(cl.size());
+    for (size_t i : evaluated) piv[i] = select(globalBC, vi, cl[i]->vertices(), cl[i]->borders());
+    const std::vector<W> intraClusterBC(globalBC);
+    std::vector<int32_t> pv;
+    std::vector<double> cards;
+    for (size_t c = 0; c < cl.size(); ++c)
+        for (size_t p = 0; p < piv[c].first.size(); ++p) {
+            pv.push_back((int32_t)piv[c].first[p]);
+            cards.push_back((double)(W)piv[c].second[p]);
+        }
+    std::vector<double> acc(n, 0.0);
+    if (!pv.empty()) dependency_batch(*d, pv, cards, o, acc);
+    for (size_t v = 0; v < n; ++v) globalBC[v] += (W)acc[v];
+    for (size_t c = 0; c < cl.size(); ++c)
+        for (size_t p = 0; p < piv[c].first.size(); ++p)
+            for (const V& v : cl[c]->vertices()) globalBC[v] -= intraClusterBC[v] * (W)(piv[c].second[p]);
+    return globalBC;
+}
+
 // The fbc CLI's result file (main.cpp:123-130, 282-294): one value per line as the stream
 // prints it, values that are not >= 0 written as 0; an existing file is refused.
 template <class W>

@@ -125,65 +125,26 @@ class GpuClusteredBrandesBC : public IBrandesBC<V, W> {
         : _gp(std::move(gp)), _ps(std::move(ps)), _o(o) {}
 
     std::vector<W> computeBC(const std::shared_ptr<const IGraph<V, W>> graph) override {
-        const size_t n = graph->vertices().size();
-        std::vector<W> globalBC(n, (W)0);
-        std::vector<std::shared_ptr<VertexInfo<V, W>>> vi(n, nullptr);
-        // Louvain on the host, as in the reference (ClusteredBrandesBC.h:80-81)
-        auto communities = _gp->partitionGraph(std::static_pointer_cast<const IDegreeGraph<V, W>>(graph));
-        std::vector<std::shared_ptr<ISubGraph<V, W>>> cl(communities.size());
-        std::vector<size_t> evaluated;
-        std::vector<std::vector<int32_t>> cv, bv;
-        for (size_t i = 0; i < cl.size(); ++i) {
-            cl[i] = std::make_shared<SubGraph<V, W>>(communities[i], graph);
 #ifdef FASTBC_BRANDES_CLUSTERED_IGNORE_UNCONNECTED
-            if (cl[i]->borders().empty()) continue;
+        const bool ignore_unconnected = true;
+#else
+        const bool ignore_unconnected = false;
 #endif
-            evaluated.push_back(i);
-            cv.emplace_back();
-            bv.emplace_back();
-            for (const V& v : cl[i]->vertices()) cv.back().push_back((int32_t)v);
-            for (const V& b : cl[i]->borders()) bv.back().push_back((int32_t)b);
-        }
-        auto d = fbcgpu::device_graph_for(*graph, _o.device);
-        // every cluster's all-sources Brandes in one call (ClusteredBrandesBC.h:91-110)
-        std::vector<double> len;
-        std::vector<uint64_t> cnt;
-        std::vector<int64_t> eo;
-        std::vector<double> intra = fbcgpu::cluster_eval_batch(*d, cv, bv, _o, &len, &cnt, &eo);
-        for (size_t k = 0; k < evaluated.size(); ++k) {
-            const size_t nb = bv[k].size();
-            for (size_t i = 0; i < cv[k].size(); ++i) {
-                const int32_t v = cv[k][i];
-                globalBC[v] += (W)intra[v];
-                vi[v] = std::make_shared<VertexInfo<V, W>>((int)nb);
-                for (size_t j = 0; j < nb; ++j) {
-                    vi[v]->setBorderSPLength((int)j, (W)len[eo[k] + i * nb + j]);
-                    vi[v]->setBorderSPCount((int)j, (V)(W)cnt[eo[k] + i * nb + j]);
-                }
-            }
-        }
-        // pivot selection on the host, in cluster order (ClusteredBrandesBC.h:112-114)
-        std::vector<std::pair<std::vector<V>, std::vector<V>>> piv(cl.size());
-        for (size_t i : evaluated)
-            piv[i] = _ps->selectPivots(globalBC, vi, cl[i]->vertices(), cl[i]->borders());
-        std::vector<W> intraClusterBC(globalBC);
-        // every pivot's full-graph dependency in one call (ClusteredBrandesBC.h:141-155)
-        std::vector<int32_t> pv;
-        std::vector<double> cards;
-        for (size_t c = 0; c < cl.size(); ++c)
-            for (size_t p = 0; p < piv[c].first.size(); ++p) {
-                pv.push_back((int32_t)piv[c].first[p]);
-                cards.push_back((double)(W)piv[c].second[p]);
-            }
-        std::vector<double> acc(n, 0.0);
-        if (!pv.empty()) fbcgpu::dependency_batch(*d, pv, cards, _o, acc);
-        for (size_t v = 0; v < n; ++v) globalBC[v] += (W)acc[v];
-        // duplicate intra-cluster dependency removed per pivot (ClusteredBrandesBC.h:158-164)
-        for (size_t c = 0; c < cl.size(); ++c)
-            for (size_t p = 0; p < piv[c].first.size(); ++p)
-                for (const V& v : cl[c]->vertices())
-                    globalBC[v] -= intraClusterBC[v] * (W)(piv[c].second[p]);
-        return globalBC;
+        // the orchestration is fbcgpu::clustered_bc; the host parts are the reference's objects
+        return fbcgpu::clustered_bc<V, W>(
+            *graph,
+            [&](const IGraph<V, W>&) {  // Louvain on the host (ClusteredBrandesBC.h:80-81)
+                return _gp->partitionGraph(std::static_pointer_cast<const IDegreeGraph<V, W>>(graph));
+            },
+            [&](const std::vector<V>& community) {
+                return std::shared_ptr<ISubGraph<V, W>>(std::make_shared<SubGraph<V, W>>(community, graph));
+            },
+            [](int nb) { return std::make_shared<VertexInfo<V, W>>(nb); },
+            [&](const std::vector<W>& bc, const std::vector<std::shared_ptr<VertexInfo<V, W>>>& vi,
+                const std::vector<V>& vertices, const std::set<V>& borders) {
+                return _ps->selectPivots(bc, vi, vertices, borders);
+            },
+            _o, ignore_unconnected);
     }
 
   private:

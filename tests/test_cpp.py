@@ -54,3 +54,36 @@ def test_reference_unit_tests_restated(fg, tmp_path):
                        timeout=300)
     assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
     assert "all passed" in r.stdout
+
+
+@pytest.mark.gpu
+def test_clustered_orchestration_runs(fg, tmp_path):
+    """fbcgpu::clustered_bc -- the code GpuClusteredBrandesBC::computeBC runs -- executed on the
+    256x256 grid with the reference's partition and k-means pivots (stand-ins return them), the
+    vertex infos written through setters with the reference's signatures; its BC equals the
+    reference's own ClusteredBrandeBC::computeBC result (|err| / max|BC| <= 1e-9)."""
+    import numpy as np
+
+    import graphs
+
+    gxx = _gxx()
+    exe = tmp_path / "clustered_run"
+    r = subprocess.run([gxx, "-std=c++17", "-O2", "-I", os.path.join(ROOT, "include"),
+                        os.path.join(ROOT, "tests", "cpp", "clustered_run.cpp"), "-L", LIBDIR, "-lfbcgpu",
+                        "-Wl,-rpath," + LIBDIR, "-o", str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-2000:]
+    z = np.load(os.path.join(GOLDEN, "grid256_clustered.npz"))
+    edges = tmp_path / "grid256.txt"
+    graphs.WORKLOADS["grid256"]().write(str(edges))
+    off, cv, poff, pv, kv = z["cluster_off"], z["cluster_vertices"], z["pivot_off"], z["pivots"], z["cards"]
+    with open(tmp_path / "clusters.txt", "w") as f:
+        for c in range(off.size - 1):
+            for a in (cv[off[c]:off[c + 1]], pv[poff[c]:poff[c + 1]], kv[poff[c]:poff[c + 1]]):
+                f.write(f"{a.size} " + " ".join(str(int(x)) for x in a) + "\n")
+    out = tmp_path / "bc.txt"
+    r = subprocess.run([str(exe), str(edges), str(tmp_path / "clusters.txt"), str(out)], capture_output=True,
+                       text=True, timeout=600)
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
+    bc = np.loadtxt(out)
+    ref = z["bc"]
+    assert np.max(np.abs(bc - ref)) / np.max(np.abs(ref)) <= 1e-9
