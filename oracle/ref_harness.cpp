@@ -12,6 +12,7 @@
 //             dumping the partition, borders, pivots and cardinalities, the intra-cluster
 //             BC and the final BC, and also runs computeBC itself to cross-check the replay.
 //   partition <edges> <seeds> <prec> <out>          LouvainGraphPartition alone: the communities
+//   select    <edges> <kfrac> <cluster.bin>...      KMeansPivotSelector on clusters evaluated elsewhere
 //   classes   <edges> <clusters> <out_prefix>       cluster evaluation + VertexInfoPivotSelector per
 //                                                   cluster (clusters file: one line per cluster,
 //                                                   "count v1 v2 ..."): exact classes' pivots/sizes
@@ -184,6 +185,54 @@ int main(int argc, char** argv) {
             std::fprintf(f, "\n");
         }
         std::fclose(f);
+        return 0;
+    }
+    if (mode == "select" && argc >= 5) {
+        // KMeansPivotSelector (VertexInfoPivotSelector + PlusPlusKMeans, KMeansPivotSelector.h:79-132)
+        // on clusters whose intra-cluster BC and border vectors were computed elsewhere (the oracle,
+        // bit-identical to DijkstraClusterEvaluator): one binary file per cluster, "int64 nc,
+        // int64 nb, int32 vertices[nc], double bc[nc], double len[nc*nb], double sigma[nc*nb]"; the
+        // borders are the reference SubGraph's own.  Prints per cluster "file count pivots..." and
+        // "count cards..." lines.
+        auto g = load(argv[2]);
+        const double kfrac = std::atof(argv[3]);
+        const size_t n = g->vertices().size();
+        for (int a = 4; a < argc; ++a) {
+            FILE* f = std::fopen(argv[a], "rb");
+            if (!f) throw std::runtime_error(std::string("cannot open ") + argv[a]);
+            int64_t nc = 0, nb = 0;
+            if (std::fread(&nc, 8, 1, f) != 1 || std::fread(&nb, 8, 1, f) != 1) throw std::runtime_error("short file");
+            std::vector<V> verts(nc);
+            std::vector<double> cbc(nc), len(nc * nb), sig(nc * nb);
+            if (std::fread(verts.data(), 4, nc, f) != (size_t)nc || std::fread(cbc.data(), 8, nc, f) != (size_t)nc ||
+                std::fread(len.data(), 8, nc * nb, f) != (size_t)(nc * nb) ||
+                std::fread(sig.data(), 8, nc * nb, f) != (size_t)(nc * nb))
+                throw std::runtime_error("short file");
+            std::fclose(f);
+            auto sg = std::make_shared<fastbc::SubGraph<V, W>>(verts, g);
+            if ((int64_t)sg->borders().size() != nb) throw std::runtime_error("border count differs");
+            std::vector<W> bc(n, 0.0);
+            std::vector<std::shared_ptr<fastbc::brandes::VertexInfo<V, W>>> vi(n, nullptr);
+            for (int64_t i = 0; i < nc; ++i) {
+                bc[verts[i]] = cbc[i];
+                vi[verts[i]] = std::make_shared<fastbc::brandes::VertexInfo<V, W>>((int)nb);
+                for (int64_t j = 0; j < nb; ++j) {
+                    // the same W -> V conversions as DijkstraClusterEvaluator.h:173-174
+                    vi[verts[i]]->setBorderSPLength((int)j, len[i * nb + j]);
+                    vi[verts[i]]->setBorderSPCount((int)j, sig[i * nb + j]);
+                }
+            }
+            fastbc::brandes::KMeansPivotSelector<V, W> ps(
+                std::shared_ptr<fastbc::brandes::IPivotSelector<V, W>>(new fastbc::brandes::VertexInfoPivotSelector<V, W>()),
+                std::shared_ptr<fastbc::kmeans::IKMeans<V, W>>(new fastbc::kmeans::PlusPlusKMeans<V, W>()), kfrac);
+            auto piv = ps.selectPivots(bc, vi, sg->vertices(), sg->borders());
+            std::printf("%s %zu", argv[a], piv.first.size());
+            for (V v : piv.first) std::printf(" %d", v);
+            std::printf("\n%zu", piv.second.size());
+            for (V k : piv.second) std::printf(" %d", k);
+            std::printf("\n");
+            std::fflush(stdout);
+        }
         return 0;
     }
     if (mode == "clustered" && argc == 7) {

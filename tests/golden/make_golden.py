@@ -14,6 +14,9 @@ oracle/_ref/ref_harness) single-threaded on the seeded workloads and stores:
   grid2048_partition.npz     LouvainGraphPartition (seeds 1-4, precision 0.01) of the
                              2048x2048 grid: community id per vertex (int16; every
                              community's vertices are ascending, as the reference lists them)
+  grid2048_pivots.npz        KMeansPivotSelector (kfrac 0.5) on three communities of that partition
+                             (5,220, 9,150 and 13,813 vertices), from the oracle's intra-cluster BC
+                             and border vectors: pivots and cardinalities per community
   DWGtext.txt                the reference unit tests' 9-vertex fixture (copied)
   rgg1500_exact_bc.txt       ExactBrandesBC<int,double> over a 1,500-point random geometric graph
                              (3-NN, weights ceil(1000 d): the family of the 48-graph batch)
@@ -29,6 +32,10 @@ minute on eight.  Usage:
   python tests/golden/make_golden.py [--reuse DIR]   (DIR: outputs of an earlier harness run)
   python tests/golden/make_golden.py --only text     (the text/ fixtures alone, seconds)
   python tests/golden/make_golden.py --only rgg      (the random-geometric-graph golden, seconds)
+  python tests/golden/make_golden.py --only c5pivots [--reuse DIR]
+                                                     (grid2048_pivots.npz: the reference's k-means
+                                                     pivot sets of three communities of the 2048x2048
+                                                     grid; hours, the communities in parallel)
 """
 from __future__ import annotations
 
@@ -145,6 +152,102 @@ def rgg_golden() -> None:
                         border_len=np.array([v[:, 0] for v in vals]), border_cnt=np.array([v[:, 1] for v in vals]))
 
 
+# Communities of the 2048x2048 grid's reference partition whose reference pivot sets are stored:
+# about the 10th, 25th and 50th percentile of the 290 communities with borders (5,220, 9,150 and
+# 13,813 vertices).  All 290 are out of reach: the reference's k-means with kfrac 0.5 runs
+# O(classes * k * borders) per Lloyd step, and a median community has 13,577 exact classes
+# (k = 6,788) over 544 borders.
+C5_CLUSTERS = (124, 199, 78)
+
+
+def c5_cluster_file(work: str, c: int, el, og, cid, isb) -> str:
+    """The oracle's DijkstraClusterEvaluator restatement (one thread: the intra BC bit-identical to
+    the reference's) on community c: vertices, intra BC, border lengths and counts in the binary
+    layout of ref_harness select."""
+    import oracle
+
+    fn = os.path.join(work, f"c{c}.bin")
+    if os.path.exists(fn):
+        return fn
+    vs = np.nonzero(cid == c)[0].astype(np.int32)
+    bs = vs[isb[vs]]
+    acc = np.zeros(el.n)
+    _, bd, bsg = oracle.cluster_eval(og, vs, bs, acc, threads=1)
+    with open(fn + ".tmp", "wb") as f:
+        f.write(np.array([vs.size, bs.size], np.int64).tobytes())
+        for a in (vs, acc[vs], bd, bsg):
+            f.write(np.ascontiguousarray(a).tobytes())
+    os.replace(fn + ".tmp", fn)
+    return fn
+
+
+def _unlimited_stack():
+    import resource
+
+    resource.setrlimit(resource.RLIMIT_STACK, (resource.RLIM_INFINITY, resource.RLIM_INFINITY))
+
+
+def _c5_select(args) -> str:
+    """ref_harness select on one community (KMeansPivotSelector, kfrac 0.5, one thread).  The
+    reference's OpenMP array reduction in PlusPlusKMeans::computeCentroids keeps a private copy on
+    the stack, which overflows the default 8 MB on these communities: the stack is unlimited."""
+    txt, fn, out = args
+    if not os.path.exists(out):
+        with open(out + ".tmp", "w") as f:
+            subprocess.run([HARNESS, "select", txt, "0.5", fn], stdout=f, check=True, env=ENV,
+                           preexec_fn=_unlimited_stack)
+        os.replace(out + ".tmp", out)
+    return out
+
+
+def read_piv(path: str):
+    with open(path) as f:
+        a, b = f.read().split("\n")[:2]
+    a = list(map(int, a.split()[1:]))
+    b = list(map(int, b.split()))
+    assert a[0] == len(a) - 1 == b[0] == len(b) - 1
+    return np.array(a[1:], np.int32), np.array(b[1:], np.int32)
+
+
+def c5_pivots(work: str) -> None:
+    """grid2048_pivots.npz: the reference's pivot sets (KMeansPivotSelector over
+    VertexInfoPivotSelector and PlusPlusKMeans, kfrac 0.5; KMeansPivotSelector.h:79-132) of the
+    C5_CLUSTERS communities of the reference partition, from their intra-cluster BC and border
+    vectors (the oracle, pinned bit-identical to DijkstraClusterEvaluator).  Up to hours per
+    community; the communities run in parallel processes."""
+    import multiprocessing as mp
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+
+    el = graphs.WORKLOADS["grid2048"]()
+    txt = os.path.join(work, "grid2048.txt")
+    if not os.path.exists(txt):
+        el.write(txt)
+    rp, col, _ = el.csr()
+    cid = np.load(os.path.join(HERE, "grid2048_partition.npz"))["community"].astype(np.int64)
+    src = np.repeat(np.arange(el.n), np.diff(rp))
+    cross = cid[src] != cid[col]
+    isb = np.zeros(el.n, bool)
+    isb[src[cross]] = True
+    isb[col[cross]] = True
+    og = oracle.CSR.from_edgelist(el)
+    jobs = [(txt, c5_cluster_file(work, c, el, og, cid, isb), os.path.join(work, f"c{c}.piv"))
+            for c in C5_CLUSTERS]
+    with mp.get_context("spawn").Pool(len(jobs)) as pool:
+        outs = pool.map(_c5_select, jobs)
+    piv, crd = [], []
+    for c, out in zip(C5_CLUSTERS, outs):
+        p, k = read_piv(out)
+        assert np.all(cid[p] == c) and int(k.sum()) == int(np.sum(cid == c))
+        piv.append(p)
+        crd.append(k)
+    off = np.zeros(len(piv) + 1, np.int64)
+    off[1:] = np.cumsum([p.size for p in piv])
+    np.savez_compressed(os.path.join(HERE, "grid2048_pivots.npz"), clusters=np.array(C5_CLUSTERS, np.int32),
+                        pivot_off=off, pivots=np.concatenate(piv), cards=np.concatenate(crd))
+
+
 def text_goldens() -> None:
     tdir = os.path.join(HERE, "text")
     os.makedirs(tdir, exist_ok=True)
@@ -158,11 +261,16 @@ def text_goldens() -> None:
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reuse", default=None)
-    ap.add_argument("--only", choices=["text", "rgg"], default=None)
+    ap.add_argument("--only", choices=["text", "rgg", "c5pivots"], default=None)
     a = ap.parse_args()
     if not REF or not os.path.isdir(os.path.join(REF, "libfastbc")):
         sys.exit("set FASTBC_REF_DIR to the reference checkout")
     subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref", f"REF={REF}"], check=True)
+    if a.only == "c5pivots":
+        work = a.reuse or tempfile.mkdtemp()
+        os.makedirs(work, exist_ok=True)
+        c5_pivots(work)
+        return
     if a.only != "rgg":
         text_goldens()
     if a.only != "text":
