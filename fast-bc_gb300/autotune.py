@@ -43,8 +43,12 @@ def _apply(choice: dict) -> dict:
 def tune_pivots(g: fg.Graph, sources, cards=None, precision: int = fg.FP32C, sample: int = 4096,
                 deltas=(2, 4, 8), threads=(64, 96, 128, 512)) -> dict:
     """Whole-graph sources (pivots, exact mode): delta (as multiples of the mean weight) and
-    the frontier kernel's block size.  Up to `sample` sources the whole list is timed, so the
-    number of waves over the concurrent slots (which the block size sets) is the real one."""
+    the frontier kernel's block size (for graphs of wide_n or more vertices, which run one
+    source per SM, the wide block size, 512 or 1024 threads, and wider buckets).  Up to `sample`
+    sources the whole list is timed, so the number of waves over the concurrent slots (which the
+    block size sets) is the real one."""
+    if g.n >= fg.get_option("wide_n"):
+        return _tune_wide(g, sources, cards, precision, sample)
     src = np.asarray(sources, np.int32)
     idx = np.linspace(0, src.size - 1, min(sample, src.size)).astype(np.int64)
     s = src[idx]
@@ -55,6 +59,23 @@ def tune_pivots(g: fg.Graph, sources, cards=None, precision: int = fg.FP32C, sam
         choice = {"delta": max(1, int(round(dm * mw))), "frontier_threads": bt}
         _apply(choice)
         t = _time(lambda st: fg.dependency_batch(g, s, c, precision, fg.BATCHED, stats=st))
+        if t < best:
+            best, arg = t, choice
+    return _apply(arg)
+
+
+def _tune_wide(g: fg.Graph, sources, cards, precision: int, sample: int,
+               deltas=(4, 8, 16), threads=(512, 1024)) -> dict:
+    src = np.asarray(sources, np.int32)
+    idx = np.linspace(0, src.size - 1, min(sample, src.size)).astype(np.int64)
+    s = src[idx]
+    c = None if cards is None else np.asarray(cards, np.float64)[idx]
+    mw = _mean_weight(g)
+    best, arg = float("inf"), None
+    for dm, bt in itertools.product(deltas, threads):
+        choice = {"delta": max(1, int(round(dm * mw))), "wide_threads": bt}
+        _apply(choice)
+        t = _time(lambda st: fg.dependency_batch(g, s, c, precision, fg.BATCHED, stats=st), reps=2)
         if t < best:
             best, arg = t, choice
     return _apply(arg)

@@ -48,6 +48,7 @@ struct Seg {
     const int2* adj;        // packed (destination, weight) pairs, rows ascending
     const int32_t* gid;     // n local -> output ids; BC index = out_base + (gid ? gid[v] : v)
     const int32_t* border;  // nb local ids of the border vertices (ascending global id)
+    const uint32_t* adj4;   // the same adjacency packed as (destination | weight << 24), or null
     int64_t out_base;
     int32_t n;              // vertices
     int32_t nb;             // border vertices (cluster segments), else 0

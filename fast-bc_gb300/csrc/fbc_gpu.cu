@@ -98,7 +98,9 @@ struct Options {
     int64_t group = 0;          // frontier kernel sources per block (1, 2, 4); 0 = automatic
     int64_t order_min_n = 131072;  // batched runs relabel graphs of at least this many vertices
     int64_t csr_device_min_m = 65536;  // edge lists of at least this many edges are built on the device
-    int64_t wide_threads = 512;        // block size of the wide frontier kernel (<= 512)
+    int64_t wide_threads = 1024;       // block size of the wide frontier kernel (<= 1024)
+    int64_t wide_kv = 1;               // level entries per lane of the 1024-thread form (1 or 2)
+    int64_t adj4 = 1;                  // use the packed 4-byte adjacency where it exists
     int64_t debug_sched = FBC_SCHED_PLAIN;  // schedule used by fbc_sssp_debug
     int64_t scratch_keep_mb = 8192;  // per-call scratch the memory pool keeps for later calls
 };
@@ -171,6 +173,7 @@ struct fbc_graph_s {
     bool ord_built = false;
     int32_t* d_ord_rp = nullptr;
     int2* d_ord_adj = nullptr;
+    uint32_t* d_ord_adj4 = nullptr;  // packed (destination | weight << 24) when n < 2^24, weights < 256
     int32_t* d_ord_inv = nullptr;
     std::vector<int32_t> ord_new;
 };
@@ -179,16 +182,17 @@ struct fbc_plan_s {
     fbc_graph_s* G = nullptr;
     int prec = FBC_PREC_FP32C;
     int64_t n = 0, ent = 0;
-    DBuf crp, cadj, cgid, cbord, segs, units, chunks, bc, bdist, bsig, ctr, retry;
+    DBuf crp, cadj, cgid, cbord, segs, units, chunks, bc, bdist, bsig, ctr, retry, bunits, ws;
     double* h_bc = nullptr;
     double* h_bdist = nullptr;
     uint64_t* h_bsig = nullptr;
     int* h_ctl = nullptr;
-    cudaGraph_t graph = nullptr;
-    cudaGraphExec_t exec = nullptr;
+    cudaGraph_t graph[2] = {nullptr, nullptr};  // resets + shared-memory kernel; frontier kernel + downloads
+    cudaGraphExec_t exec[2] = {nullptr, nullptr};
     bool captured = false;
-    double relax = 0, bytes = 0;
-    int64_t nunits = 0;
+    double relax = 0, wbytes = 0, bbytes = 0;
+    int64_t nunits = 0, wunits = 0, bunits_n = 0;
+    int launches = 0;
     std::vector<int64_t> coff, boff;
     std::vector<int32_t> cverts, borders;
     // frees everything the plan holds, also when its creation stopped half way
@@ -198,9 +202,12 @@ struct fbc_plan_s {
             dg_.enter();
             cudaStreamSynchronize(g.st);
         }
-        if (exec) cudaGraphExecDestroy(exec);
-        if (graph) cudaGraphDestroy(graph);
-        for (DBuf* b : {&crp, &cadj, &cgid, &cbord, &segs, &units, &chunks, &bc, &bdist, &bsig, &ctr, &retry})
+        for (int i = 0; i < 2; ++i) {
+            if (exec[i]) cudaGraphExecDestroy(exec[i]);
+            if (graph[i]) cudaGraphDestroy(graph[i]);
+        }
+        for (DBuf* b : {&crp, &cadj, &cgid, &cbord, &segs, &units, &chunks, &bc, &bdist, &bsig, &ctr, &retry,
+                        &bunits, &ws})
             b->release();
         if (h_bc) cudaFreeHost(h_bc);
         if (h_bdist) cudaFreeHost(h_bdist);
@@ -406,6 +413,14 @@ int ensure_order(fbc_graph_s* G) {
     FBC_CK(cudaMemcpyAsync(G->d_ord_rp, rp32.data(), sizeof(int32_t) * rp32.size(), cudaMemcpyHostToDevice, g.st));
     FBC_CK(cudaMemcpyAsync(G->d_ord_adj, adj.data(), sizeof(int2) * adj.size(), cudaMemcpyHostToDevice, g.st));
     FBC_CK(cudaMemcpyAsync(G->d_ord_inv, inv.data(), sizeof(int32_t) * inv.size(), cudaMemcpyHostToDevice, g.st));
+    std::vector<uint32_t> adj4;
+    if (n < (1 << 24) && G->maxw < 256) {
+        adj4.resize(adj.size());
+        for (size_t k = 0; k < adj.size(); ++k) adj4[k] = (uint32_t)adj[k].x | ((uint32_t)adj[k].y << 24);
+        FBC_CK(cudaMalloc(&G->d_ord_adj4, sizeof(uint32_t) * adj4.size()));
+        FBC_CK(cudaMemcpyAsync(G->d_ord_adj4, adj4.data(), sizeof(uint32_t) * adj4.size(), cudaMemcpyHostToDevice,
+                               g.st));
+    }
     FBC_CK(cudaStreamSynchronize(g.st));
     G->ord_new = std::move(nw);
     G->ord_built = true;
@@ -466,15 +481,30 @@ int64_t ws_budget() {
 using KernFn = void (*)(fbc::KParams);
 
 template <class Prec>
-KernFn frontier_variant(bool wide, int K) {
-    if (wide) {
-        if (K == 4) return fbc::frontier_kernel<Prec, true, 4>;
-        if (K == 2) return fbc::frontier_kernel<Prec, true, 2>;
-        return fbc::frontier_kernel<Prec, true, 1>;
+KernFn frontier_variant(bool wide, int K, int threads, bool a4) {
+    if (a4 && wide && K == 1) {  // one source per block on a packed adjacency
+        if (threads > 512) return g.opt.wide_kv == 1 ? fbc::frontier_kernel<Prec, 3, 1, true>
+                                                     : fbc::frontier_kernel<Prec, 2, 1, true>;
+        return fbc::frontier_kernel<Prec, 1, 1, true>;
     }
-    if (K == 4) return fbc::frontier_kernel<Prec, false, 4>;
-    if (K == 2) return fbc::frontier_kernel<Prec, false, 2>;
-    return fbc::frontier_kernel<Prec, false, 1>;
+    if (wide && threads > 512 && g.opt.wide_kv == 1) {
+        if (K == 4) return fbc::frontier_kernel<Prec, 3, 4>;
+        if (K == 2) return fbc::frontier_kernel<Prec, 3, 2>;
+        return fbc::frontier_kernel<Prec, 3, 1>;
+    }
+    if (wide && threads > 512) {
+        if (K == 4) return fbc::frontier_kernel<Prec, 2, 4>;
+        if (K == 2) return fbc::frontier_kernel<Prec, 2, 2>;
+        return fbc::frontier_kernel<Prec, 2, 1>;
+    }
+    if (wide) {
+        if (K == 4) return fbc::frontier_kernel<Prec, 1, 4>;
+        if (K == 2) return fbc::frontier_kernel<Prec, 1, 2>;
+        return fbc::frontier_kernel<Prec, 1, 1>;
+    }
+    if (K == 4) return fbc::frontier_kernel<Prec, 0, 4>;
+    if (K == 2) return fbc::frontier_kernel<Prec, 0, 2>;
+    return fbc::frontier_kernel<Prec, 0, 1>;
 }
 
 // Units of each segment in groups of K (a segment's last group padded with src = -1).
@@ -490,12 +520,20 @@ std::vector<Unit> group_units(const std::vector<Unit>& units, int K) {
     return out;
 }
 
-// Block-per-source launch with global-memory slots.  Plain schedule: brandes_block_kernel;
-// batched schedule: frontier_kernel, K sources of one segment per block.
+// Launch configuration of a block-per-source launch with global-memory slots.  Plain schedule:
+// brandes_block_kernel; batched schedule: frontier_kernel, K sources of one segment per block.
+struct BlockCfg {
+    KernFn kern = nullptr;
+    bool fr = false;           // frontier kernel (else the plain block kernel)
+    int K = 1, threads = 0;
+    int64_t stride = 0, slots = 0;
+    int32_t cnt_bits = 8;
+    std::vector<Unit> units;   // grouped by K (K > 1: each segment's last group padded)
+};
+
 template <class Prec>
-int launch_block(const Plan& P, const std::vector<Unit>& units_in, int ws_n, fbc_stats* st,
-                 int& launches, bool force_plain = false, bool sig_f64 = false) {
-    if (units_in.empty()) return FBC_OK;
+int block_config(const Plan& P, const std::vector<Unit>& units_in, int ws_n, bool force_plain, bool sig_f64,
+                 int64_t budget, BlockCfg& c) {
     const bool fr = P.sched == FBC_SCHED_BATCHED && !force_plain && !sig_f64;
     // wide blocks for segments of millions of vertices (their frontiers are hundreds wide)
     const bool wide = fr && (g.opt.frontier_threads > 128 || (int64_t)ws_n >= g.opt.wide_n);
@@ -509,11 +547,9 @@ int launch_block(const Plan& P, const std::vector<Unit>& units_in, int ws_n, fbc
         const int na = P.segs[a.seg].n, nb = P.segs[b.seg].n;
         return na != nb ? na > nb : a.seg < b.seg;
     });
-    KernFn kern = nullptr;
-    int Kg = 1, bps = 1;
-    int64_t stride = 0, slots = 0;
-    std::vector<Unit> units;
-    const int64_t budget = ws_budget();
+    c = BlockCfg{};
+    c.fr = fr;
+    c.threads = threads;
     if (fr) {
         // sources per block (option "group" forces one): sharing rounds and levels pays where
         // a source's frontier is much narrower than the block -- segments of up to 32K
@@ -522,10 +558,12 @@ int launch_block(const Plan& P, const std::vector<Unit>& units_in, int ws_n, fbc
         // for every block slot.
         const int forced = (int)g.opt.group;
         const int cand[3] = {4, 2, 1};
+        bool a4 = true;  // every segment of the launch has the packed adjacency
+        for (const Unit& u : sorted) a4 = a4 && P.segs[u.seg].adj4 != nullptr;
         for (int K : cand) {
             if (forced > 0 ? K != forced : (K > 1 && ws_n > 32768)) continue;
             if ((int64_t)ws_n * K >= ((int64_t)1 << 31) - 1) continue;
-            KernFn f = frontier_variant<Prec>(wide, K);
+            KernFn f = frontier_variant<Prec>(wide, K, threads, a4);
             int b = 0;
             FBC_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, f, threads, 0));
             b = std::max(b, 1);
@@ -537,52 +575,61 @@ int launch_block(const Plan& P, const std::vector<Unit>& units_in, int ws_n, fbc
             const int64_t sl = std::max<int64_t>(1, std::min<int64_t>(std::min(full, groups), budget / strd));
             const bool ok = K == 1 || forced > 0 || (groups >= full && sl >= full);
             if (!ok) continue;
-            kern = f;
-            Kg = K;
-            bps = b;
-            stride = strd;
-            slots = sl;
-            units.swap(gu);
+            c.kern = f;
+            c.K = K;
+            c.stride = strd;
+            c.slots = sl;
+            c.units.swap(gu);
             break;
         }
-    } else {
-        const int64_t sb = fbc::state_bytes<Prec>(ws_n);
-        stride = 256 + ((sb + 255) & ~int64_t(255));
-        kern = sig_f64 ? fbc::brandes_block_kernel<Prec, true> : fbc::brandes_block_kernel<Prec>;
-        FBC_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kern, threads, 0));
-        bps = std::max(bps, 1);
-        slots = std::min<int64_t>((int64_t)g.nsm * bps, (int64_t)sorted.size());
-        slots = std::max<int64_t>(1, std::min<int64_t>(slots, budget / stride));
-        units.swap(sorted);
-    }
-    if (!kern) return fail(FBC_ERR_INVALID_ARG, "no frontier kernel variant fits this segment");
-    // the two kernels keep different between-unit invariants: never share a workspace
-    Workspace& W = fr ? g.wsw : g.wsb;
-    FBC_TRY(ensure_ws(W, slots, stride, ws_n * Kg, (int)sizeof(typename Prec::D)));
-    FBC_CK(g.units_b.ensure(sizeof(Unit) * units.size()));
-    FBC_CK(cudaMemcpyAsync(g.units_b.p, units.data(), sizeof(Unit) * units.size(),
-                           cudaMemcpyHostToDevice, g.st));
-    if (st) st->h2d_bytes += (int64_t)(sizeof(Unit) * units.size());
-    KParams K = base_params(P);
-    K.units = g.units_b.as<Unit>();
-    K.nunits = (int64_t)units.size() / Kg;
-    if (fr) {
         // 8-bit counters (path counts up to 2^56) when no vertex of the launch's segments has
         // 255 or more in-edges, else 16-bit (the host keeps segments of 65,535+ off this kernel)
         int32_t maxin = 0;
-        for (const Unit& u : units) maxin = std::max(maxin, P.seg_maxindeg[u.seg]);
-        K.cnt_bits = maxin < 255 ? 8 : 16;
+        for (const Unit& u : c.units) maxin = std::max(maxin, P.seg_maxindeg[u.seg]);
+        c.cnt_bits = maxin < 255 ? 8 : 16;
+    } else {
+        const int64_t sb = fbc::state_bytes<Prec>(ws_n);
+        c.stride = 256 + ((sb + 255) & ~int64_t(255));
+        c.kern = sig_f64 ? fbc::brandes_block_kernel<Prec, true> : fbc::brandes_block_kernel<Prec>;
+        int bps = 1;
+        FBC_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, c.kern, threads, 0));
+        bps = std::max(bps, 1);
+        c.slots = std::min<int64_t>((int64_t)g.nsm * bps, (int64_t)sorted.size());
+        c.slots = std::max<int64_t>(1, std::min<int64_t>(c.slots, budget / c.stride));
+        c.units.swap(sorted);
     }
+    if (!c.kern) return fail(FBC_ERR_INVALID_ARG, "no frontier kernel variant fits this segment");
+    return FBC_OK;
+}
+
+// Block-per-source launch on the library's workspace.
+template <class Prec>
+int launch_block(const Plan& P, const std::vector<Unit>& units_in, int ws_n, fbc_stats* st,
+                 int& launches, bool force_plain = false, bool sig_f64 = false) {
+    if (units_in.empty()) return FBC_OK;
+    BlockCfg c;
+    FBC_TRY(block_config<Prec>(P, units_in, ws_n, force_plain, sig_f64, ws_budget(), c));
+    // the two kernels keep different between-unit invariants: never share a workspace
+    Workspace& W = c.fr ? g.wsw : g.wsb;
+    FBC_TRY(ensure_ws(W, c.slots, c.stride, ws_n * c.K, (int)sizeof(typename Prec::D)));
+    FBC_CK(g.units_b.ensure(sizeof(Unit) * c.units.size()));
+    FBC_CK(cudaMemcpyAsync(g.units_b.p, c.units.data(), sizeof(Unit) * c.units.size(),
+                           cudaMemcpyHostToDevice, g.st));
+    if (st) st->h2d_bytes += (int64_t)(sizeof(Unit) * c.units.size());
+    KParams K = base_params(P);
+    K.units = g.units_b.as<Unit>();
+    K.nunits = (int64_t)c.units.size() / c.K;
+    if (c.fr) K.cnt_bits = c.cnt_bits;
     K.next_unit = g.ctr.as<unsigned long long>() + 0;
     K.ws = W.buf.as<char>();
     K.ws_stride = W.stride;
     K.ws_n = (int32_t)W.ws_n;  // block kernel: vertices; frontier kernel: entries (v*K + k)
-    kern<<<(unsigned)slots, threads, 0, g.st>>>(K);
+    c.kern<<<(unsigned)c.slots, c.threads, 0, g.st>>>(K);
     FBC_CK(cudaGetLastError());
     ++launches;
     if (st) {
-        st->slots = (int32_t)slots;
-        st->group = Kg;
+        st->slots = (int32_t)c.slots;
+        st->group = c.K;
     }
     return FBC_OK;
 }
@@ -1378,7 +1425,9 @@ int fbc_set_option(const char* key, int64_t value) {
     else if (k == "ws_budget_mb") g.opt.ws_budget_mb = std::max<int64_t>(0, value);
     else if (k == "order_min_n") g.opt.order_min_n = std::max<int64_t>(0, value);
     else if (k == "csr_device_min_m") g.opt.csr_device_min_m = std::max<int64_t>(0, value);
-    else if (k == "wide_threads") g.opt.wide_threads = std::max<int64_t>(64, std::min<int64_t>(512, value / 32 * 32));
+    else if (k == "wide_threads") g.opt.wide_threads = std::max<int64_t>(64, std::min<int64_t>(1024, value / 32 * 32));
+    else if (k == "wide_kv") g.opt.wide_kv = value <= 1 ? 1 : 2;
+    else if (k == "adj4") g.opt.adj4 = value != 0;
     else if (k == "group") {
         if (value != 0 && value != 1 && value != 2 && value != 4) return fail(FBC_ERR_INVALID_ARG, "group must be 0, 1, 2 or 4");
         g.opt.group = value;
@@ -1411,6 +1460,8 @@ int fbc_get_option(const char* key, int64_t* value) {
     else if (k == "order_min_n") *value = g.opt.order_min_n;
     else if (k == "csr_device_min_m") *value = g.opt.csr_device_min_m;
     else if (k == "wide_threads") *value = g.opt.wide_threads;
+    else if (k == "wide_kv") *value = g.opt.wide_kv;
+    else if (k == "adj4") *value = g.opt.adj4;
     else if (k == "debug_sched") *value = g.opt.debug_sched;
     else if (k == "scratch_keep_mb") *value = g.opt.scratch_keep_mb;
     else return fail(FBC_ERR_INVALID_ARG, "unknown option " + k);
@@ -1591,6 +1642,7 @@ int batched_graph_seg(fbc_graph_s* G, int64_t out_base, int sched, Seg& s, const
     FBC_TRY(ensure_order(G));
     s.rp = G->d_ord_rp;
     s.adj = G->d_ord_adj;
+    s.adj4 = g.opt.adj4 ? G->d_ord_adj4 : nullptr;
     s.gid = G->d_ord_inv;
     map = G->ord_new.data();
     return FBC_OK;
@@ -1608,6 +1660,7 @@ int fbc_graph_free(fbc_graph G) {
     cudaFree(G->d_adj);
     if (G->d_ord_rp) cudaFree(G->d_ord_rp);
     if (G->d_ord_adj) cudaFree(G->d_ord_adj);
+    if (G->d_ord_adj4) cudaFree(G->d_ord_adj4);
     if (G->d_ord_inv) cudaFree(G->d_ord_inv);
     delete G;
     return FBC_OK;
@@ -1869,7 +1922,8 @@ int fbc_cluster_eval_batch(fbc_graph G, int32_t nclusters, const int64_t* coff,
     FBC_TRY(check_init(dg_));
     if (!G) return fail(FBC_ERR_INVALID_ARG, "null graph");
     FBC_TRY(check_sched(sched));
-    if (border_off && !borders) return fail(FBC_ERR_INVALID_ARG, "border_off without borders");
+    if (border_off && !borders && nclusters > 0 && border_off[nclusters] > 0)
+        return fail(FBC_ERR_INVALID_ARG, "border_off without borders");
     const double t0 = now_ms();
     if (st) std::memset(st, 0, sizeof(*st));
     Plan P;
@@ -1889,6 +1943,137 @@ int fbc_cluster_eval_batch(fbc_graph G, int32_t nclusters, const int64_t* coff,
     if (st) st->wall_ms = now_ms() - t0;
     return FBC_OK;
 }
+
+}  // extern "C"
+
+namespace {
+// Capture of a prepared cluster sweep: counter and accumulator resets, the shared-memory kernel
+// for the communities that fit it, the frontier kernel (four sources per block) for the larger
+// ones on a workspace of the plan's own, and the downloads into pinned memory, as two CUDA graphs
+// replayed back to back (an event between them times the two kernels apart).  Communities that
+// need the plain kernels (above 32K vertices, in-degrees of 65,535 or more) leave the plan
+// uncaptured: fbc_plan_run then takes the general path.
+template <class Prec>
+int plan_capture(fbc_plan_s* p, Plan& P) {
+    std::vector<char> small(P.segs.size(), 0);
+    for (size_t s = 0; s < P.segs.size(); ++s)
+        small[s] = P.segs[s].n <= std::min<int64_t>(g.opt.warp_max_n, 65535) && P.seg_maxw[s] < 65536 &&
+                   P.seg_m[s] < ((int64_t)1 << 30);
+    for (;;) {  // the shared-memory layout fits at least two warps of the largest small segment
+        int nm = 0, mm = 0, arg = -1;
+        for (size_t s = 0; s < P.segs.size(); ++s)
+            if (small[s]) {
+                mm = std::max<int>(mm, (int)P.seg_m[s]);
+                if (P.segs[s].n >= nm) { nm = P.segs[s].n; arg = (int)s; }
+            }
+        if (arg < 0 || small_fits(nm, mm, 2)) break;
+        small[arg] = 0;
+    }
+    std::vector<std::vector<Unit>> by_seg(P.segs.size());
+    std::vector<Unit> uw, ub;
+    int nw_max = 0, mw_max = 0, nw_min = 1 << 30, nb_max = 0;
+    for (const Unit& u : P.units) {
+        const Seg& sg = P.segs[u.seg];
+        if (small[u.seg]) {
+            by_seg[u.seg].push_back(u);
+            nw_max = std::max(nw_max, sg.n);
+            nw_min = std::min(nw_min, sg.n);
+            mw_max = std::max<int>(mw_max, (int)P.seg_m[u.seg]);
+        } else {
+            if (sg.n > 32768 || P.seg_maxindeg[u.seg] >= 65535) return FBC_OK;  // general path
+            ub.push_back(u);
+            nb_max = std::max(nb_max, sg.n);
+        }
+    }
+    for (auto& v : by_seg) uw.insert(uw.end(), v.begin(), v.end());
+    std::stable_sort(ub.begin(), ub.end(), [&](const Unit& a, const Unit& b) { return P.segs[a.seg].n > P.segs[b.seg].n; });
+    const size_t n8 = sizeof(double) * (size_t)std::max<int64_t>(p->n, 1);
+    const size_t e8 = 8 * (size_t)std::max<int64_t>(p->ent, 1);
+    FBC_CK(p->segs.ensure(sizeof(Seg) * P.segs.size()));
+    FBC_CK(p->bc.ensure(n8));
+    FBC_CK(p->bdist.ensure(e8));
+    FBC_CK(p->bsig.ensure(e8));
+    FBC_CK(p->ctr.ensure(64));
+    FBC_CK(p->retry.ensure(sizeof(fbc::RetryRec) * P.units.size()));
+    FBC_CK(cudaMemcpyAsync(p->segs.p, P.segs.data(), sizeof(Seg) * P.segs.size(), cudaMemcpyHostToDevice, g.st));
+    KParams base{};
+    base.segs = p->segs.as<Seg>();
+    base.bc = p->bc.as<double>();
+    base.bdist = p->bdist.as<double>();
+    base.bsig = p->bsig.as<unsigned long long>();
+    base.err = (int*)(p->ctr.as<unsigned long long>() + 2);
+    base.retry_count = base.err + 1;
+    base.retry = p->retry.as<fbc::RetryRec>();
+    base.retry_cap = (int32_t)P.units.size();
+    base.iter_mult = (int32_t)g.opt.iter_mult;
+    SmallCfg cfg;
+    fbc::SmallParams S{};
+    if (!uw.empty()) {
+        FBC_TRY(small_config(P, uw, nw_max, mw_max, nw_min, cfg));
+        FBC_CK(p->units.ensure(sizeof(Unit) * uw.size()));
+        FBC_CK(p->chunks.ensure(sizeof(fbc::Chunk) * cfg.chunks.size()));
+        FBC_CK(cudaMemcpyAsync(p->units.p, uw.data(), sizeof(Unit) * uw.size(), cudaMemcpyHostToDevice, g.st));
+        FBC_CK(cudaMemcpyAsync(p->chunks.p, cfg.chunks.data(), sizeof(fbc::Chunk) * cfg.chunks.size(),
+                               cudaMemcpyHostToDevice, g.st));
+        S.k = base;
+        S.k.units = p->units.as<Unit>();
+        S.k.nunits = (int64_t)uw.size();
+        S.chunks = p->chunks.as<fbc::Chunk>();
+        S.nchunks = (int32_t)cfg.chunks.size();
+        S.nmax = nw_max;
+        S.mmax = mw_max;
+        S.smem = (int32_t)cfg.dyn;
+        S.next_chunk = p->ctr.as<unsigned long long>() + 1;
+        FBC_CK(cudaFuncSetAttribute(fbc::small_seg_kernel<Prec>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cfg.dyn));
+    }
+    BlockCfg bc;
+    KParams K = base;
+    if (!ub.empty()) {
+        FBC_TRY(block_config<Prec>(P, ub, nb_max, false, false, ws_budget(), bc));
+        if (!bc.fr) return FBC_OK;
+        FBC_CK(p->bunits.ensure(sizeof(Unit) * bc.units.size()));
+        FBC_CK(cudaMemcpyAsync(p->bunits.p, bc.units.data(), sizeof(Unit) * bc.units.size(), cudaMemcpyHostToDevice,
+                               g.st));
+        FBC_CK(p->ws.ensure((size_t)(bc.slots * bc.stride), true, g.st));  // zeroed: fresh slots
+        K.units = p->bunits.as<Unit>();
+        K.nunits = (int64_t)bc.units.size() / bc.K;
+        K.cnt_bits = bc.cnt_bits;
+        K.next_unit = p->ctr.as<unsigned long long>() + 0;
+        K.ws = p->ws.as<char>();
+        K.ws_stride = bc.stride;
+        K.ws_n = (int32_t)(nb_max * bc.K);
+    }
+    FBC_CK(cudaStreamSynchronize(g.st));
+    for (const Unit& u : uw) p->wbytes += 40.0 * (double)P.seg_m[u.seg] + 52.0 * P.segs[u.seg].n;
+    for (const Unit& u : ub) p->bbytes += 40.0 * (double)P.seg_m[u.seg] + 52.0 * P.segs[u.seg].n;
+    p->wunits = (int64_t)uw.size();
+    p->bunits_n = (int64_t)ub.size();
+    p->launches = (uw.empty() ? 0 : 1) + (ub.empty() ? 0 : 1);
+    FBC_CK(cudaStreamBeginCapture(g.st, cudaStreamCaptureModeThreadLocal));
+    cudaMemsetAsync(p->ctr.p, 0, 64, g.st);
+    cudaMemsetAsync(p->bc.p, 0, n8, g.st);
+    if (!uw.empty()) fbc::small_seg_kernel<Prec><<<(unsigned)cfg.blocks, 32 * cfg.wpb, (size_t)cfg.dyn, g.st>>>(S);
+    cudaError_t ce = cudaStreamEndCapture(g.st, &p->graph[0]);
+    if (ce != cudaSuccess) return fail(FBC_ERR_CUDA, std::string("capture: ") + cudaGetErrorString(ce));
+    FBC_CK(cudaGraphInstantiate(&p->exec[0], p->graph[0], 0));
+    FBC_CK(cudaStreamBeginCapture(g.st, cudaStreamCaptureModeThreadLocal));
+    if (!ub.empty()) bc.kern<<<(unsigned)bc.slots, bc.threads, 0, g.st>>>(K);
+    cudaMemcpyAsync(p->h_bc, p->bc.p, n8, cudaMemcpyDeviceToHost, g.st);
+    if (p->ent > 0) {
+        cudaMemcpyAsync(p->h_bdist, p->bdist.p, e8, cudaMemcpyDeviceToHost, g.st);
+        cudaMemcpyAsync(p->h_bsig, p->bsig.p, e8, cudaMemcpyDeviceToHost, g.st);
+    }
+    cudaMemcpyAsync(p->h_ctl, (char*)p->ctr.p + 16, 8, cudaMemcpyDeviceToHost, g.st);
+    ce = cudaStreamEndCapture(g.st, &p->graph[1]);
+    if (ce != cudaSuccess) return fail(FBC_ERR_CUDA, std::string("capture: ") + cudaGetErrorString(ce));
+    FBC_CK(cudaGraphInstantiate(&p->exec[1], p->graph[1], 0));
+    p->captured = true;
+    return FBC_OK;
+}
+
+}  // namespace
+
+extern "C" {
 
 int fbc_cluster_plan_create(fbc_graph G, int32_t nclusters, const int64_t* coff, const int32_t* cverts,
                             const int64_t* border_off, const int32_t* borders, int precision,
@@ -1913,19 +2098,7 @@ int fbc_cluster_plan_create(fbc_graph G, int32_t nclusters, const int64_t* coff,
     Plan P;
     FBC_TRY(prepare_clusters(G, nclusters, coff, cverts, border_off, borders, precision, FBC_SCHED_BATCHED,
                              p->crp, p->cadj, p->cgid, p->cbord, P, p->ent, nullptr));
-    int nmax = 0, mmax = 0, nmin = 1 << 30;
-    bool small = true;
-    for (size_t k = 0; k < P.segs.size(); ++k) {
-        small = small && P.segs[k].n <= std::min<int64_t>(g.opt.warp_max_n, 65535) && P.seg_maxw[k] < 65536;
-        nmax = std::max(nmax, P.segs[k].n);
-        mmax = std::max<int>(mmax, (int)P.seg_m[k]);
-        if (P.segs[k].n > 0) nmin = std::min(nmin, P.segs[k].n);
-    }
-    small = small && !P.units.empty() && small_fits(nmax, mmax, 2);
-    for (const Unit& u : P.units) {
-        p->relax += (double)P.seg_m[u.seg];
-        p->bytes += 40.0 * (double)P.seg_m[u.seg] + 52.0 * P.segs[u.seg].n;
-    }
+    for (const Unit& u : P.units) p->relax += (double)P.seg_m[u.seg];
     p->nunits = (int64_t)P.units.size();
     const size_t n8 = sizeof(double) * (size_t)std::max<int64_t>(p->n, 1);
     const size_t e8 = 8 * (size_t)std::max<int64_t>(p->ent, 1);
@@ -1933,58 +2106,9 @@ int fbc_cluster_plan_create(fbc_graph G, int32_t nclusters, const int64_t* coff,
     FBC_CK(cudaMallocHost(&p->h_bdist, e8));
     FBC_CK(cudaMallocHost(&p->h_bsig, e8));
     FBC_CK(cudaMallocHost(&p->h_ctl, 64));
-    if (small) {
-        SmallCfg cfg;
-        FBC_TRY(small_config(P, P.units, nmax, mmax, nmin, cfg));
-        FBC_CK(p->segs.ensure(sizeof(Seg) * P.segs.size()));
-        FBC_CK(p->units.ensure(sizeof(Unit) * P.units.size()));
-        FBC_CK(p->chunks.ensure(sizeof(fbc::Chunk) * cfg.chunks.size()));
-        FBC_CK(p->bc.ensure(n8));
-        FBC_CK(p->bdist.ensure(e8));
-        FBC_CK(p->bsig.ensure(e8));
-        FBC_CK(p->ctr.ensure(64));
-        FBC_CK(p->retry.ensure(sizeof(fbc::RetryRec) * P.units.size()));
-        FBC_CK(cudaMemcpyAsync(p->segs.p, P.segs.data(), sizeof(Seg) * P.segs.size(), cudaMemcpyHostToDevice, g.st));
-        FBC_CK(cudaMemcpyAsync(p->units.p, P.units.data(), sizeof(Unit) * P.units.size(), cudaMemcpyHostToDevice, g.st));
-        FBC_CK(cudaMemcpyAsync(p->chunks.p, cfg.chunks.data(), sizeof(fbc::Chunk) * cfg.chunks.size(),
-                               cudaMemcpyHostToDevice, g.st));
-        FBC_CK(cudaStreamSynchronize(g.st));
-        fbc::SmallParams S{};
-        S.k.segs = p->segs.as<Seg>();
-        S.k.units = p->units.as<Unit>();
-        S.k.nunits = (int64_t)P.units.size();
-        S.k.bc = p->bc.as<double>();
-        S.k.bdist = p->bdist.as<double>();
-        S.k.bsig = p->bsig.as<unsigned long long>();
-        S.k.err = (int*)(p->ctr.as<unsigned long long>() + 2);
-        S.k.retry_count = S.k.err + 1;
-        S.k.retry = p->retry.as<fbc::RetryRec>();
-        S.k.retry_cap = (int32_t)P.units.size();
-        S.k.iter_mult = (int32_t)g.opt.iter_mult;
-        S.chunks = p->chunks.as<fbc::Chunk>();
-        S.nchunks = (int32_t)cfg.chunks.size();
-        S.nmax = nmax;
-        S.mmax = mmax;
-        S.smem = (int32_t)cfg.dyn;
-        S.next_chunk = p->ctr.as<unsigned long long>() + 1;
-        const bool f64 = precision == FBC_PREC_FP64;
-        if (f64) FBC_CK(cudaFuncSetAttribute(fbc::small_seg_kernel<fbc::PrecF64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cfg.dyn));
-        else FBC_CK(cudaFuncSetAttribute(fbc::small_seg_kernel<fbc::PrecDF32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cfg.dyn));
-        // capture: reset counters and the BC accumulator, run the sweep, download into pinned memory
-        FBC_CK(cudaStreamBeginCapture(g.st, cudaStreamCaptureModeThreadLocal));
-        cudaMemsetAsync(p->ctr.p, 0, 64, g.st);
-        cudaMemsetAsync(p->bc.p, 0, n8, g.st);
-        if (f64) fbc::small_seg_kernel<fbc::PrecF64><<<(unsigned)cfg.blocks, 32 * cfg.wpb, (size_t)cfg.dyn, g.st>>>(S);
-        else fbc::small_seg_kernel<fbc::PrecDF32><<<(unsigned)cfg.blocks, 32 * cfg.wpb, (size_t)cfg.dyn, g.st>>>(S);
-        cudaMemcpyAsync(p->h_bc, p->bc.p, n8, cudaMemcpyDeviceToHost, g.st);
-        if (p->ent > 0) {
-            cudaMemcpyAsync(p->h_bdist, p->bdist.p, e8, cudaMemcpyDeviceToHost, g.st);
-            cudaMemcpyAsync(p->h_bsig, p->bsig.p, e8, cudaMemcpyDeviceToHost, g.st);
-        }
-        cudaMemcpyAsync(p->h_ctl, (char*)p->ctr.p + 16, 8, cudaMemcpyDeviceToHost, g.st);
-        FBC_CK(cudaStreamEndCapture(g.st, &p->graph));
-        FBC_CK(cudaGraphInstantiate(&p->exec, p->graph, 0));
-        p->captured = true;
+    if (!P.units.empty()) {
+        if (precision == FBC_PREC_FP64) FBC_TRY(plan_capture<fbc::PrecF64>(p, P));
+        else FBC_TRY(plan_capture<fbc::PrecDF32>(p, P));
     }
     *out = guard.release();
     return FBC_OK;
@@ -1999,19 +2123,26 @@ int fbc_plan_run(fbc_plan p, fbc_stats* st) {
     if (st) std::memset(st, 0, sizeof(*st));
     if (p->captured) {
         FBC_CK(cudaEventRecord(g.ev0, g.st));
-        FBC_CK(cudaGraphLaunch(p->exec, g.st));
+        FBC_CK(cudaGraphLaunch(p->exec[0], g.st));
+        FBC_CK(cudaEventRecord(g.evm, g.st));
+        FBC_CK(cudaGraphLaunch(p->exec[1], g.st));
         FBC_CK(cudaEventRecord(g.ev1, g.st));
         FBC_CK(cudaStreamSynchronize(g.st));
         if (p->h_ctl[0] == 0 && p->h_ctl[1] == 0) {
             if (st) {
-                float ms = 0.f;
+                float ms = 0.f, mw = 0.f;
                 FBC_CK(cudaEventElapsedTime(&ms, g.ev0, g.ev1));
+                FBC_CK(cudaEventElapsedTime(&mw, g.ev0, g.evm));
                 st->kernel_ms = ms;
-                st->warp_ms = ms;
-                st->units = st->warp_units = p->nunits;
+                st->warp_ms = p->wunits ? mw : 0.0;
+                st->block_ms = p->bunits_n ? ms - mw : 0.0;
+                st->units = p->nunits;
+                st->warp_units = p->wunits;
+                st->block_units = p->bunits_n;
                 st->relaxations = p->relax;
-                st->warp_bytes = p->bytes;
-                st->launches = 1;
+                st->warp_bytes = p->wbytes;
+                st->block_bytes = p->bbytes;
+                st->launches = p->launches;
                 st->d2h_bytes = 8 * (p->n + 2 * p->ent);
                 st->wall_ms = now_ms() - t0;
             }

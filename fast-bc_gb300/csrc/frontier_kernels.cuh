@@ -156,7 +156,20 @@ __device__ __forceinline__ void bpush(bool want, const E& x, E* q, int* c, int c
 // in flight together; 4 measured slower, spilling at the register caps); kE:
 // queued entries per lane in the distance pass (1: two measured slower on the wide blocks,
 // which then spill at their 128-register cap).
-template <class Prec, int kV, int K, int kE>
+// One adjacency entry (destination, weight): from the int2 array, or with kA4 from the packed
+// 4-byte form (destination in the low 24 bits, weight in the high 8), which halves the bytes
+// of every row access.
+template <bool kA4>
+__device__ __forceinline__ int2 adj_at(const Seg& sg, int e) {
+    if constexpr (kA4) {
+        const uint32_t u = __ldg(sg.adj4 + e);
+        return make_int2((int)(u & 0xffffffu), (int)(u >> 24));
+    } else {
+        return __ldg(sg.adj + e);
+    }
+}
+
+template <class Prec, int kV, int K, int kE, bool kA4>
 __device__ void frontier_group(const KParams& P, const Unit* us, const FState<Prec>& S, FCtl& C,
                                int64_t cap) {
     static_assert(K == 1 || K == 2 || K == 4 || K == 8, "K is a power of two up to 8");
@@ -165,7 +178,6 @@ __device__ void frontier_group(const KParams& P, const Unit* us, const FState<Pr
     const int n = sg.n;
     const int nK = n * K;
     const int* __restrict__ rp = sg.rp;
-    const int2* __restrict__ adj = sg.adj;
     const int delta = sg.delta > 0 ? sg.delta : 1;
     const int tid = threadIdx.x, nth = blockDim.x;
     const int qc_cap = (int)fqcap(cap);
@@ -231,7 +243,7 @@ __device__ void frontier_group(const KParams& P, const Unit* us, const FState<Pr
                         const int j = t / 4, q = t % 4;
                         x[t] = -1;
                         if (e[j] + q < e1[j]) {
-                            const int2 a = __ldg(adj + e[j] + q);
+                            const int2 a = adj_at<kA4>(sg, e[j] + q);
                             x[t] = (a.x << kSh) + kk[j];
                             nd[t] = dv[j] + a.y;
                             r0[t] = __ldg(rp + a.x);  // x's row, in flight with the atomic
@@ -341,7 +353,7 @@ __device__ void frontier_group(const KParams& P, const Unit* us, const FState<Pr
                 for (int j = 0; j < 4; ++j) {
                     x[j] = -1;
                     if (e[j] < e1[j]) {
-                        const int2 a = __ldg(adj + e[j]++);
+                        const int2 a = adj_at<kA4>(sg, e[j]++);
                         x[j] = (a.x << kSh) + ((v0 + j * nth) & (K - 1));
                         nd[j] = dv[j] + a.y;
                         any = true;
@@ -428,7 +440,7 @@ __device__ void frontier_group(const KParams& P, const Unit* us, const FState<Pr
                             ei = e[j]++;
                         }
                         if (ei >= 0) {
-                            const int2 a = __ldg(adj + ei);
+                            const int2 a = adj_at<kA4>(sg, ei);
                             x[j] = (a.x << kSh) + kk[j];
                             nd[j] = dv[j] + a.y;
                             r0[j] = __ldg(rp + a.x);  // row offsets: small and shared, L2-resident
@@ -521,7 +533,7 @@ __device__ void frontier_group(const KParams& P, const Unit* us, const FState<Pr
                         if (mk[j]) {
                             const int b = __ffs(mk[j]) - 1;
                             mk[j] &= mk[j] - 1u;
-                            x[j] = (__ldg(adj + o[j].e0 + b).x << kSh) + (o[j].v & (K - 1));
+                            x[j] = (adj_at<kA4>(sg, o[j].e0 + b).x << kSh) + (o[j].v & (K - 1));
                         }
                     }
                     unsigned long long sx[kV];
@@ -550,7 +562,7 @@ __device__ void frontier_group(const KParams& P, const Unit* us, const FState<Pr
                         const int dv = dist_of(ldcg64(S.word + o[j].v));
                         const unsigned long long sv = o[j].sigdm >> pk.cb;
                         for (int e = o[j].e0; e < e1; ++e) {
-                            const int2 a = __ldg(adj + e);
+                            const int2 a = adj_at<kA4>(sg, e);
                             const int xk = (a.x << kSh) + k;
                             if (dv + a.y == dist_of(ldcg64(S.word + xk))) {
                                 const ulonglong2 r = __ldcg(reinterpret_cast<const ulonglong2*>(S.rec + xk));
@@ -597,11 +609,14 @@ __device__ void frontier_group(const KParams& P, const Unit* us, const FState<Pr
     __syncthreads();
 }
 
-// kWide: 512-thread blocks for segments whose frontiers span many hundreds of vertices
-// (millions of vertices); otherwise 128-thread blocks, five per SM.  K: sources per block;
-// units come in groups of K of one segment (padded with src = -1), P.nunits counts groups.
-template <class Prec, bool kWide, int K>
-__global__ void __launch_bounds__(kWide ? 512 : 128, kWide ? 1 : 5) frontier_kernel(KParams P) {
+// kForm: 0 = 128-thread blocks, five per SM; 1 = 512-thread blocks for segments whose frontiers
+// span many hundreds of vertices (millions of vertices); 2 = 1024-thread blocks (64 registers),
+// two level entries per lane; 3 = the same with one level entry per lane (fewer spills).
+// K: sources per block; units come in groups of K of one segment (padded with src = -1),
+// P.nunits counts groups.  kA4: the segments' packed 4-byte adjacency.
+template <class Prec, int kForm, int K, bool kA4 = false>
+__global__ void __launch_bounds__(kForm >= 2 ? 1024 : kForm == 1 ? 512 : 128, kForm == 0 ? 5 : 1)
+    frontier_kernel(KParams P) {
     __shared__ FCtl C;
     __shared__ Unit us[K];
     char* slot = P.ws + (int64_t)blockIdx.x * P.ws_stride;
@@ -623,7 +638,7 @@ __global__ void __launch_bounds__(kWide ? 512 : 128, kWide ? 1 : 5) frontier_ker
         if (gi < P.nunits && threadIdx.x < K) us[threadIdx.x] = P.units[gi * K + threadIdx.x];
         __syncthreads();
         if (gi >= P.nunits) break;
-        frontier_group<Prec, 2, K, 1>(P, us, S, C, cap);
+        frontier_group<Prec, kForm == 3 ? 1 : 2, K, 1, kA4>(P, us, S, C, cap);
     }
 }
 

@@ -329,7 +329,8 @@ def cluster_eval_batch(g: Graph, cs: ClusterSet, precision: int = FP64, sched: i
 
 class ClusterPlan:
     """A prepared cluster sweep (fbc_cluster_plan_create): the cluster subgraphs are uploaded
-    once and each run() replays a captured CUDA graph of the shared-memory kernel."""
+    once and each run() replays captured CUDA graphs of the sweep's kernels (the shared-memory
+    kernel and/or the frontier kernel, by community size)."""
 
     def __init__(self, g: Graph, cs: ClusterSet, precision: int = FP64):
         self.g = g

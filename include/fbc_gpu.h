@@ -87,7 +87,11 @@ const char* fbc_last_error_string(void);
  *   "group"            sources per frontier block: 1, 2, 4, or 0 = automatic (others refused)
  *   "chunk_max"        sources per work item of the shared-memory kernel
  *   "wide_n"           segments of at least this many vertices use the wide frontier blocks
- *   "wide_threads"     block size of the wide frontier blocks (64..512, a multiple of 32)
+ *   "wide_threads"     block size of the wide frontier blocks (64..1024, a multiple of 32; above 512
+ *                      a 1024-thread form with 64 registers per thread; default 1024)
+ *   "wide_kv"          level entries per lane of the 1024-thread form: 1 (default) or 2
+ *   "adj4"             1 (default): wide one-source blocks on a relabelled graph with fewer than 2^24
+ *                      vertices and weights below 256 read its adjacency packed in 4 bytes; 0: 8 bytes
  *   "warp_max_n"       largest segment run warp-per-source in shared memory
  *   "order_min_n"      batched runs relabel graphs of at least this many vertices for memory
  *                      locality (outputs stay in input ids)
@@ -172,10 +176,12 @@ int fbc_cluster_eval_batch(fbc_graph g, int32_t nclusters, const int64_t* cluste
 
 /* Prepared cluster sweep for repeated evaluation of the same clusters (the Louvain-cluster
  * sweep of the clustered mode): the cluster subgraphs, units and work items are uploaded once
- * and the sweep (counter resets, the shared-memory kernel, downloads into pinned host buffers)
- * is captured into a CUDA graph; fbc_plan_run replays it.  Clusters that do not fit the
- * shared-memory kernel, or a run whose path counts need a wider representation, are evaluated
- * with fbc_cluster_eval_batch instead (same results).  fbc_plan_results gives host views of the
+ * and the sweep (counter resets, the shared-memory kernel for the clusters that fit it, the
+ * frontier kernel -- four sources per block, on a workspace of the plan's own -- for the larger
+ * ones, downloads into pinned host buffers) is captured into CUDA graphs; fbc_plan_run replays
+ * them.  A plan with a cluster of more than 32,768 vertices (or a vertex of 65,535+ in-edges) is
+ * not captured, and a run whose path counts need a wider representation is redone: both are
+ * evaluated with fbc_cluster_eval_batch instead (same results).  fbc_plan_results gives host views of the
  * last run's intra-cluster BC (n entries, overwritten each run) and border vectors (layout of
  * fbc_cluster_eval_batch), valid until the next run or fbc_plan_free. */
 typedef struct fbc_plan_s* fbc_plan;

@@ -73,6 +73,27 @@ def test_c5_clusters_match_oracle(fg, c5):
             assert np.array_equal(ev.border_sigma[e0:e1].reshape(-1, nb).astype(np.float64), bs)
 
 
+def test_c5_cluster_plan_captured(fg, c5):
+    """The same three communities as a prepared sweep: the frontier-kernel launch is captured, and
+    every replay equals the direct batched evaluation (border vectors bit-exact, intra BC within the
+    precision form's bound)."""
+    el, g, og, order, off = c5
+    picks = _clusters(off, order)
+    cs = fg.ClusterSet.from_lists([order[off[c]:off[c + 1]] for c in picks]).with_borders(g)
+    for prec, tol in ((fg.FP64, TOL_FP64), (fg.FP32C, TOL_FP32C)):
+        base = fg.cluster_eval_batch(g, cs, prec, fg.BATCHED)
+        plan = fg.ClusterPlan(g, cs, prec)
+        assert plan.captured
+        for _ in range(2):
+            st = fg.Stats()
+            ev = plan.run(st)
+            assert st.launches == 1 and st.block_units == cs.vertices.size
+            assert rel_err(ev.intra_bc, base.intra_bc) <= tol
+            assert np.array_equal(ev.border_dist, base.border_dist)
+            assert np.array_equal(ev.border_sigma, base.border_sigma)
+        plan.free()
+
+
 def test_c5_pivots_match_oracle(fg, c5):
     el, g, og, order, off = c5
     src = np.unique(graphs.rand_int(23, 5, np.arange(16), 0, el.n - 1)).astype(np.int32)

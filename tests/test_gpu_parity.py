@@ -263,35 +263,38 @@ def test_grid256_cluster_border_vectors(fg):
 
 @pytest.mark.parametrize("prec", [0, 1])
 def test_cluster_plan_replays(fg, prec):
-    """A prepared sweep (captured CUDA graph) gives the reference's intra BC and bit-exact border
-    vectors on every replay; with the shared-memory kernel ruled out it takes the general path
-    and gives the same results."""
+    """A prepared sweep (captured CUDA graphs) gives the reference's intra BC and bit-exact border
+    vectors on every replay, whichever kernels it captures: the shared-memory kernel alone (the
+    default for these communities), both kernels (communities on either side of warp_max_n), or
+    the frontier kernel alone (four sources per block).  A community above 32K vertices keeps the
+    plan uncaptured: it runs the general path with the same results."""
     z, keep, cs, piv, crd = _clustered_inputs(fg)
     g = fg.Graph.from_edgelist(graphs.WORKLOADS["grid256"]())
     tol = TOL_FP64 if prec == 0 else TOL_FP32C
     base = fg.cluster_eval_batch(g, cs, prec, fg.PLAIN)
-    plan = fg.ClusterPlan(g, cs, prec)
-    assert plan.captured
-    for _ in range(3):
-        st = fg.Stats()
-        ev = plan.run(st)
-        assert st.launches == 1 and st.units == cs.vertices.size
-        assert rel_err(ev.intra_bc, z["intra_bc"]) <= tol
-        assert np.array_equal(ev.border_dist, base.border_dist)
-        assert np.array_equal(ev.border_sigma, base.border_sigma)
-    plan.free()
     old = fg.get_option("warp_max_n")
-    fg.set_option("warp_max_n", 64)
     try:
-        plan = fg.ClusterPlan(g, cs, prec)
-        assert not plan.captured
-        ev = plan.run()
-        assert rel_err(ev.intra_bc, z["intra_bc"]) <= tol
-        assert np.array_equal(ev.border_dist, base.border_dist)
-        assert np.array_equal(ev.border_sigma, base.border_sigma)
-        plan.free()
+        for wmax, launches in ((old, 1), (900, 2), (64, 1)):
+            fg.set_option("warp_max_n", wmax)
+            plan = fg.ClusterPlan(g, cs, prec)
+            assert plan.captured
+            for _ in range(3):
+                st = fg.Stats()
+                ev = plan.run(st)
+                assert st.launches == launches and st.units == cs.vertices.size
+                assert (st.block_units > 0) == (wmax < old) and (st.warp_units > 0) == (wmax > 64)
+                assert rel_err(ev.intra_bc, z["intra_bc"]) <= tol
+                assert np.array_equal(ev.border_dist, base.border_dist)
+                assert np.array_equal(ev.border_sigma, base.border_sigma)
+            plan.free()
     finally:
         fg.set_option("warp_max_n", old)
+    whole = fg.ClusterSet.from_lists([np.arange(g.n, dtype=np.int32)]).with_borders(g)
+    plan = fg.ClusterPlan(g, whole, prec)
+    assert not plan.captured
+    ev = plan.run()
+    ref = fg.cluster_eval_batch(g, whole, prec, fg.BATCHED)
+    assert rel_err(ev.intra_bc, ref.intra_bc) <= tol
 
 
 @pytest.mark.parametrize("sched", [0, 1])
