@@ -54,6 +54,14 @@ int orc_cluster_eval(int32_t n, const int64_t* row_ptr, const int32_t* col, cons
                      int32_t nverts, const int32_t* verts, int32_t nborders, const int32_t* borders,
                      double* bc_accum, double* bdist, double* bsigma, int nthreads);
 
+/* The k-means step of the pivot selection for one cluster (kmeans_oracle.c): np exact-class
+ * pivots with normalized border vectors L[np*b] (lengths) and Cn[np*b] (counts) and class sizes
+ * wt[np]; k = max(floor(np * kfrac), 1) centroids, at most max_iter + 1 Lloyd steps.  Writes the
+ * distinct chosen pivots as indices into the class list (out_idx) with their weights (out_w), in
+ * centroid order, and returns how many; out_idx and out_w have room for k entries. */
+int32_t orc_kmeans_pivots(int32_t np, int32_t b, const double* L, const int32_t* Cn, const int32_t* wt,
+                          double kfrac, int32_t max_iter, int32_t* out_idx, int32_t* out_w);
+
 /* Pivot scatter (ClusteredBrandesBC.h:147-155): bc_accum[v] += dep_p[v] * card[p]. */
 int orc_pivot_batch(int32_t n, const int64_t* row_ptr, const int32_t* col, const double* w,
                     int64_t npiv, const int32_t* pivots, const double* card, double* bc_accum,

@@ -30,6 +30,8 @@ def lib():
         L.orc_sssp_dump.restype = i64
         L.orc_cluster_eval.argtypes = [i32, vp, vp, vp, i32, vp, i32, vp, vp, vp, vp, C.c_int]
         L.orc_pivot_batch.argtypes = [i32, vp, vp, vp, i64, vp, vp, vp, C.c_int]
+        L.orc_kmeans_pivots.argtypes = [i32, i32, vp, vp, vp, C.c_double, i32, vp, vp]
+        L.orc_kmeans_pivots.restype = i32
         _lib = L
     return _lib
 
@@ -112,3 +114,19 @@ def pivot_batch(g: CSR, pivots, cards, bc_accum=None, threads: int = 1):
         bc_accum = np.zeros(max(g.n, 1))
     assert lib().orc_pivot_batch(*g.args(), p.size, _p(p), _p(c), _p(bc_accum), threads) == 0
     return bc_accum
+
+
+def kmeans_pivots(lengths, counts, weights, kfrac: float = 0.5, max_iter: int = 100):
+    """KMeansPivotSelector's k-means step on one cluster's exact classes: lengths / counts are the
+    class pivots' normalized border vectors (np x b), weights the class sizes.  Returns (indices
+    into the class list, weights) of the distinct chosen pivots."""
+    L = np.ascontiguousarray(lengths, np.float64)
+    Cn = np.ascontiguousarray(counts, np.int32)
+    w = np.ascontiguousarray(weights, np.int32)
+    npv = L.shape[0]
+    b = L.shape[1] if L.ndim == 2 else 0
+    k = max(int(npv * kfrac), 1)
+    idx = np.zeros(k, np.int32)
+    ow = np.zeros(k, np.int32)
+    cnt = lib().orc_kmeans_pivots(npv, b, _p(L), _p(Cn), _p(w), kfrac, max_iter, _p(idx), _p(ow))
+    return idx[:cnt], ow[:cnt]
