@@ -20,6 +20,7 @@ def test_reference_arm_json_line():
                 "scaling", "vs_baseline", "dtype", "data", "config", "impl", "cpu_baseline", "e2e"):
         assert key in line, key
     assert line["impl"] == "reference" and line["unit"] == "GTEPS" and line["value"] > 0
-    assert line["config"]["workload"].startswith("clustered fast-bc, 256x256 road grid")
+    assert line["config"]["workload"].startswith("clustered fast-bc, 2048x2048 road grid")
+    assert line["config"]["pivots"] > 0 and line["config"]["kfrac"] == 0.5
     assert line["cpu_baseline"]["kind"] in ("port", "reference") and line["cpu_baseline"]["cores"] >= 1
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["d2h_bytes_per_step"] == 0
