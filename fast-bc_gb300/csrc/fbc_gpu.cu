@@ -24,6 +24,7 @@
 #include "graph_build.cuh"
 #include "text_parse.cuh"
 #include "frontier_kernels.cuh"
+#include "kmeans.cuh"
 
 namespace {
 
@@ -1774,6 +1775,94 @@ int fbc_cluster_borders(fbc_graph G, int32_t nclusters, const int64_t* coff, con
     FBC_TRY(device_borders(G, nclusters, coff, boff, bl, nullptr));
     if (out_boff) std::copy(boff.begin(), boff.end(), out_boff);
     if (out_borders) std::copy(bl.begin(), bl.end(), out_borders);
+    return FBC_OK;
+}
+
+int fbc_kmeans(int32_t nsets, const int64_t* set_off, const int32_t* nb, const int64_t* vec_off, const double* len,
+               const int32_t* cnt, const int32_t* wt, const int32_t* k, double min_variance, int32_t max_iter,
+               int32_t* out_idx, int32_t* out_w, fbc_stats* st) {
+    std::lock_guard<std::recursive_mutex> lk(g_mu);
+    DevGuard dg_;
+    FBC_TRY(check_init(dg_));
+    if (nsets < 0 || (nsets > 0 && (!set_off || !nb || !vec_off || !k || !wt || !out_idx || !out_w)))
+        return fail(FBC_ERR_INVALID_ARG, "null argument");
+    if (max_iter < 0) return fail(FBC_ERR_INVALID_ARG, "max_iter < 0");
+    const double t0 = now_ms();
+    if (st) std::memset(st, 0, sizeof(*st));
+    if (nsets == 0) return FBC_OK;
+    // sets, their points as (length, count) int pairs transposed per set (border-major), work areas
+    std::vector<fbc::KMSet> sets((size_t)nsets);
+    int64_t xs = 0, ws = 0, outs = 0;
+    for (int32_t s = 0; s < nsets; ++s) {
+        const int64_t np = set_off[s + 1] - set_off[s];
+        if (np <= 0 || np > 0x7fffffff || nb[s] < 0 || k[s] < 1 || k[s] > np)
+            return fail(FBC_ERR_INVALID_ARG, "set " + std::to_string(s) + ": needs 1 <= k <= points, nb >= 0");
+        if (nb[s] > 0 && (!len || !cnt)) return fail(FBC_ERR_INVALID_ARG, "null vectors");
+        fbc::KMSet& S = sets[(size_t)s];
+        S.np = (int32_t)np;
+        S.nb = nb[s];
+        S.k = k[s];
+        S.x_off = xs;
+        S.ws_off = ws;
+        S.out_off = outs;
+        S.p_off = set_off[s];
+        xs += np * nb[s];
+        ws += fbc::km_work_bytes(np, nb[s], k[s]);
+        outs += k[s];
+    }
+    std::vector<int2> X((size_t)std::max<int64_t>(xs, 1));
+    for (int32_t s = 0; s < nsets; ++s) {
+        const fbc::KMSet& S = sets[(size_t)s];
+        double lmax = 0.0, cmax = 0.0;
+        for (int64_t j = 0; j < S.np; ++j)
+            for (int32_t i = 0; i < S.nb; ++i) {
+                const double l = len[vec_off[s] + j * S.nb + i];
+                const int32_t c = cnt[vec_off[s] + j * S.nb + i];
+                if (!(l >= 0.0 && l <= 2147483647.0) || l != std::floor(l))
+                    return fail(FBC_ERR_INVALID_ARG, "lengths must be integers in [0, 2^31)");
+                lmax = std::max(lmax, l);
+                cmax = std::max(cmax, std::fabs((double)c));
+                X[(size_t)(S.x_off + (int64_t)i * S.np + j)] = make_int2((int32_t)l, c);
+            }
+        // every squared distance exact in a double, as the reference's sums are on these inputs
+        if ((double)S.nb * (lmax * lmax + 4.0 * cmax * cmax) >= 9007199254740992.0)
+            return fail(FBC_ERR_RANGE, "set " + std::to_string(s) + ": squared distances may exceed 2^53");
+    }
+    TmpBuf dsets, dx, dwt, dws, didx, dw;
+    FBC_CK(dsets.ensure(sizeof(fbc::KMSet) * sets.size()));
+    FBC_CK(dx.ensure(sizeof(int2) * X.size()));
+    FBC_CK(dwt.ensure(sizeof(int32_t) * (size_t)set_off[nsets]));
+    FBC_CK(dws.ensure((size_t)std::max<int64_t>(ws, 256)));
+    FBC_CK(didx.ensure(sizeof(int32_t) * (size_t)outs));
+    FBC_CK(dw.ensure(sizeof(int32_t) * (size_t)outs));
+    FBC_CK(cudaMemcpyAsync(dsets.p, sets.data(), sizeof(fbc::KMSet) * sets.size(), cudaMemcpyHostToDevice, g.st));
+    FBC_CK(cudaMemcpyAsync(dx.p, X.data(), sizeof(int2) * X.size(), cudaMemcpyHostToDevice, g.st));
+    FBC_CK(cudaMemcpyAsync(dwt.p, wt, sizeof(int32_t) * (size_t)set_off[nsets], cudaMemcpyHostToDevice, g.st));
+    fbc::KMParams K{};
+    K.sets = dsets.as<fbc::KMSet>();
+    K.X = dx.as<int2>();
+    K.wt = dwt.as<int32_t>();
+    K.ws = dws.as<char>();
+    K.min_variance = min_variance;
+    K.max_iter = max_iter;
+    K.out_idx = didx.as<int32_t>();
+    K.out_w = dw.as<int32_t>();
+    FBC_CK(cudaEventRecord(g.ev0, g.st));
+    fbc::kmeans_kernel<<<(unsigned)nsets, 1024, 0, g.st>>>(K);
+    FBC_CK(cudaGetLastError());
+    FBC_CK(cudaEventRecord(g.ev1, g.st));
+    FBC_CK(cudaMemcpyAsync(out_idx, didx.p, sizeof(int32_t) * (size_t)outs, cudaMemcpyDeviceToHost, g.st));
+    FBC_CK(cudaMemcpyAsync(out_w, dw.p, sizeof(int32_t) * (size_t)outs, cudaMemcpyDeviceToHost, g.st));
+    FBC_CK(cudaStreamSynchronize(g.st));
+    if (st) {
+        float ms = 0.f;
+        FBC_CK(cudaEventElapsedTime(&ms, g.ev0, g.ev1));
+        st->kernel_ms = ms;
+        st->launches = 1;
+        st->h2d_bytes = (int64_t)(sizeof(int2) * X.size() + sizeof(int32_t) * set_off[nsets]);
+        st->d2h_bytes = (int64_t)(8 * outs);
+        st->wall_ms = now_ms() - t0;
+    }
     return FBC_OK;
 }
 

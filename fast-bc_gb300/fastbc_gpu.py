@@ -93,6 +93,7 @@ def _load():
         "fbc_plan_run": ([vp, P(Stats)], C.c_int),
         "fbc_plan_results": ([vp, P(vp), P(vp), P(vp), P(i64), P(i32)], C.c_int),
         "fbc_plan_free": ([vp], C.c_int),
+        "fbc_kmeans": ([i32, vp, vp, vp, vp, vp, vp, vp, dbl, i32, vp, vp, P(Stats)], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)
@@ -393,6 +394,62 @@ def cluster_classes(g: Graph, cs: ClusterSet, bc, ev: ClusterEval):
                                 _ptr(bcv), _ptr(np.ascontiguousarray(bd)), _ptr(np.ascontiguousarray(bs)),
                                 _ptr(coff), _ptr(piv), _ptr(crd)))
     return [(piv[coff[c]:coff[c + 1]].copy(), crd[coff[c]:coff[c + 1]].copy()) for c in range(cs.count)]
+
+
+def kmeans(sets, kfrac: float = 0.5, max_iter: int = 100, min_variance: float = 0.0,
+           stats: Stats | None = None):
+    """PlusPlusKMeans::computeCentroids on the device for several point sets at once (fbc_kmeans).
+    `sets`: (lengths np x nb, counts np x nb, weights np) per set, the normalized border vectors of
+    the exact classes' pivots and the class sizes; k = max(int(np * kfrac), 1) as
+    KMeansPivotSelector chooses it.  Returns per set (centroid point indices, weights), duplicates
+    kept."""
+    nsets = len(sets)
+    set_off = np.zeros(nsets + 1, np.int64)
+    nb = np.zeros(max(nsets, 1), np.int32)
+    vec_off = np.zeros(max(nsets, 1), np.int64)
+    ks = np.zeros(max(nsets, 1), np.int32)
+    Ls, Cs, Ws = [], [], []
+    vo = 0
+    for s, (L, Cn, w) in enumerate(sets):
+        L = np.ascontiguousarray(L, np.float64)
+        npv = L.shape[0]
+        set_off[s + 1] = set_off[s] + npv
+        nb[s] = L.shape[1] if L.ndim == 2 else 0
+        vec_off[s] = vo
+        vo += L.size
+        ks[s] = max(int(npv * kfrac), 1)
+        Ls.append(L.ravel())
+        Cs.append(np.ascontiguousarray(Cn, np.int32).ravel())
+        Ws.append(np.ascontiguousarray(w, np.int32))
+    Lf = np.concatenate(Ls) if vo else np.zeros(1)
+    Cf = np.concatenate(Cs) if vo else np.zeros(1, np.int32)
+    Wf = np.concatenate(Ws) if nsets else np.zeros(1, np.int32)
+    kout = np.zeros(max(int(ks[:nsets].sum()), 1), np.int32)
+    wout = np.zeros_like(kout)
+    _ck(lib.fbc_kmeans(nsets, _ptr(set_off), _ptr(nb), _ptr(vec_off), _ptr(Lf), _ptr(Cf), _ptr(Wf), _ptr(ks),
+                       float(min_variance), int(max_iter), _ptr(kout), _ptr(wout), _stats(stats)))
+    out, o = [], 0
+    for s in range(nsets):
+        out.append((kout[o:o + ks[s]].copy(), wout[o:o + ks[s]].copy()))
+        o += ks[s]
+    return out
+
+
+def kmeans_pivot_sets(class_pivots, sets, kfrac: float = 0.5, max_iter: int = 100):
+    """KMeansPivotSelector::selectPivots after the exact classes (KMeansPivotSelector.h:92-130):
+    the device k-means, then duplicate pivots removed keeping the first; `class_pivots[s]` maps a
+    set's point index to its vertex.  Returns per set (pivots, weights)."""
+    res = []
+    for cp, (idx, w) in zip(class_pivots, kmeans(sets, kfrac, max_iter)):
+        seen, pv, pw = set(), [], []
+        for i, x in zip(idx.tolist(), w.tolist()):
+            if i in seen:
+                continue
+            seen.add(i)
+            pv.append(int(cp[i]))
+            pw.append(x)
+        res.append((np.array(pv, np.int32), np.array(pw, np.int32)))
+    return res
 
 
 def multi_exact_bc(graphs: list[Graph], precision: int = FP64, sched: int = BATCHED,

@@ -400,6 +400,42 @@ std::vector<W> clustered_bc(const G& graph, Partition&& partition, MakeCluster&&
     return globalBC;
 }
 
+// PlusPlusKMeans::computeCentroids (PlusPlusKMeans.h:76-147) on the device for one point set:
+// `vertices` index `vi` (objects with borders(), getBorderSPLength(j), getBorderSPCount(j), as
+// VertexInfo); returns the k centroids (vertices, duplicates kept) and their weights, as the
+// reference's does.
+template <class V, class W, class VIPtr>
+std::pair<std::vector<V>, std::vector<V>> kmeans_centroids(int k, const std::vector<V>& vertices,
+                                                           const std::vector<V>& weights, const std::vector<VIPtr>& vi,
+                                                           W min_variance, size_t max_iteration, int device = 0) {
+    ensure_device(device);
+    const size_t np = vertices.size();
+    const int32_t nb = np ? (int32_t)vi[vertices[0]]->borders() : 0;
+    std::vector<double> len(np * (size_t)nb);
+    std::vector<int32_t> cnt(np * (size_t)nb), wt(np);
+    for (size_t j = 0; j < np; ++j) {
+        const auto& p = vi[vertices[j]];
+        if (p->borders() != nb) throw Error(FBC_ERR_INVALID_ARG, "libfbcgpu: vertex infos of different sizes");
+        for (int32_t i = 0; i < nb; ++i) {
+            len[j * nb + i] = (double)p->getBorderSPLength(i);
+            cnt[j * nb + i] = (int32_t)p->getBorderSPCount(i);
+        }
+        wt[j] = (int32_t)weights[j];
+    }
+    std::pair<std::vector<V>, std::vector<V>> out;
+    if (np == 0) return out;
+    const int64_t set_off[2] = {0, (int64_t)np}, vec_off[1] = {0};
+    const int32_t kk = (int32_t)k;
+    std::vector<int32_t> idx((size_t)k), w((size_t)k);
+    check(fbc_kmeans(1, set_off, &nb, vec_off, len.data(), cnt.data(), wt.data(), &kk, (double)min_variance,
+                     (int32_t)std::min<size_t>(max_iteration, 0x7fffffff), idx.data(), w.data(), nullptr));
+    for (int c = 0; c < k; ++c) {
+        out.first.push_back(vertices[(size_t)idx[(size_t)c]]);
+        out.second.push_back((V)w[(size_t)c]);
+    }
+    return out;
+}
+
 // The fbc CLI's result file (main.cpp:123-130, 282-294): one value per line as the stream
 // prints it, values that are not >= 0 written as 0; an existing file is refused.
 template <class W>

@@ -14,6 +14,8 @@
 //                                                reference's own selector for inputs outside the
 //                                                clustered pipeline's shape); usable as the
 //                                                exact selector inside KMeansPivotSelector
+//   GpuPlusPlusKMeans       : kmeans::IKMeans    replaces PlusPlusKMeans (PlusPlusKMeans.h:76-147) inside
+//                                                KMeansPivotSelector: the same centroids and weights
 //   GpuClusteredBrandesBC   : IBrandesBC         ClusteredBrandeBC (ClusteredBrandesBC.h:63-169)
 //                             with one GPU call for all clusters and one for all pivots; the
 //                             partition and pivot selection are the caller's reference objects.
@@ -154,4 +156,26 @@ class GpuClusteredBrandesBC : public IBrandesBC<V, W> {
 };
 
 }  // namespace brandes
+
+namespace kmeans {
+
+template <typename V, typename W>
+class GpuPlusPlusKMeans : public IKMeans<V, W> {
+  public:
+    explicit GpuPlusPlusKMeans(fbcgpu::Options o = {}) : _o(o) {}
+    std::pair<std::vector<V>, std::vector<V>> computeCentroids(
+        int k, const std::vector<V>& vertices, const std::vector<V>& weights,
+        const std::vector<std::shared_ptr<brandes::VertexInfo<V, W>>>& vertexInfo, W minVariance = 0,
+        size_t maxIteration = 100) override {
+        std::lock_guard<std::mutex> lk(_mu);  // pivot selection may run on OpenMP workers
+        return fbcgpu::kmeans_centroids<V, W>(k, vertices, weights, vertexInfo, minVariance, maxIteration, _o.device);
+    }
+
+  private:
+    fbcgpu::Options _o;
+    std::mutex _mu;
+};
+
+}  // namespace kmeans
+
 }  // namespace fastbc

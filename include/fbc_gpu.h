@@ -207,6 +207,24 @@ int fbc_cluster_classes(fbc_graph g, int32_t nclusters, const int64_t* cluster_o
                         const double* bc, const double* border_dist, const uint64_t* border_sigma,
                         int64_t* out_class_off, int32_t* out_pivots, int32_t* out_cards);
 
+/* The k-means step of the clustered pivot selection (PlusPlusKMeans::computeCentroids,
+ * PlusPlusKMeans.h:76-147, as KMeansPivotSelector.h:95-100 calls it) for nsets independent point
+ * sets at once, one thread block each.  Set s has np_s = set_off[s+1] - set_off[s] points of
+ * nb[s] entries: point j's lengths len[vec_off[s] + j*nb[s] + i] (integers in [0, 2^31): a
+ * normalized border vector, VertexInfo::normalize) and counts cnt[...] (the int border path counts
+ * VertexInfo stores), weight wt[set_off[s] + j]; k[s] centroids (1 <= k <= np_s).  The reference's
+ * arithmetic and tie rules are kept (k-means++ start, each point to its first nearest centroid,
+ * each centroid to the first member nearest to the members' mean, stop when no centroid moves by
+ * more than min_variance or after max_iter + 1 steps), so the result equals the reference's
+ * single-threaded one.  Outputs for set s at o_s = k[0] + ... + k[s-1]: out_idx[o_s + c] the point
+ * index (within the set) of centroid c, duplicates kept as computeCentroids returns them
+ * (KMeansPivotSelector removes them), out_w[o_s + c] the summed weights of its members in the last
+ * step.  FBC_ERR_RANGE when a squared distance could pass 2^53 (the reference's double sums would
+ * then round). */
+int fbc_kmeans(int32_t nsets, const int64_t* set_off, const int32_t* nb, const int64_t* vec_off, const double* len,
+               const int32_t* cnt, const int32_t* wt, const int32_t* k, double min_variance, int32_t max_iter,
+               int32_t* out_idx, int32_t* out_w, fbc_stats* st);
+
 /* Exact BC of several independent graphs in one persistent launch.  out_bc[g] has
  * n_g entries. */
 int fbc_multi_exact_bc(int32_t ngraphs, const fbc_graph* graphs, int precision, int sched,

@@ -46,6 +46,11 @@ int main(int argc, char** argv) {
         std::shared_ptr<kmeans::IKMeans<V, W>>(new kmeans::PlusPlusKMeans<V, W>()), 0.5);
     std::shared_ptr<IBrandesBC<V, W>> batched_gps = std::make_shared<GpuClusteredBrandesBC<V, W>>(gp, gps, o);
     (void)batched_gps;
+    // and the k-means step on the device too
+    std::shared_ptr<IPivotSelector<V, W>> gkm = std::make_shared<KMeansPivotSelector<V, W>>(
+        std::make_shared<GpuVertexInfoPivotSelector<V, W>>(o),
+        std::make_shared<kmeans::GpuPlusPlusKMeans<V, W>>(o), 0.5);
+    (void)gkm;
     if (argc > 2) {
         std::string mode = argv[2];
         std::vector<W> bc = mode == "exact" ? exact->computeBC(graph)
