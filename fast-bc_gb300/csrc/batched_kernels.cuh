@@ -322,7 +322,7 @@ __device__ void small_unit(const KParams& K, const Seg& sg, const Unit& u, const
             for (int j = lane; j < sg.nb; j += 32) {
                 const int b = sg.border[j];
                 const int d = dist[b];
-                K.bdist[u.bout + j] = d != kInf ? (double)d : 0.0;
+                K.bdist[u.bout + j] = d != kInf ? nonneg_int_to_double(d) : 0.0;
                 K.bsig[u.bout + j] = sig_get(slo, shi, b);
             }
         }
@@ -330,6 +330,7 @@ __device__ void small_unit(const KParams& K, const Seg& sg, const Unit& u, const
     if (!bad) {
         // --------------------------------------------------------- dependency
         const double card = u.card;
+        const bool card1 = card == 1.0;  // one FP64 compare per unit, not per vertex
         for (int L = nlev - 1; L >= 0; --L) {
             const int a1 = lvl[L + 1];
             for (int i = lvl[L] + lane; i < a1; i += 32) {
@@ -362,8 +363,9 @@ __device__ void small_unit(const KParams& K, const Seg& sg, const Unit& u, const
                 }
                 dlt[v] = Prec::store(acc);
                 if (v != src) {
-                    const double c = card == 1.0 ? Prec::value(acc) : card * Prec::value(acc);
-                    atomicAdd(K.bc + sg.out_base + (sg.gid ? sg.gid[v] : v), c);
+                    double* o = K.bc + sg.out_base + (sg.gid ? sg.gid[v] : v);
+                    if (card1) Prec::red_add(o, acc);
+                    else atomicAdd(o, card * Prec::value(acc));
                 }
             }
             __syncwarp();

@@ -130,6 +130,34 @@ __device__ __forceinline__ unsigned long long ld_u64(const unsigned long long* p
     else return __ldcg(p);
 }
 
+// ------------------------------------------------------------ FP64 values from integer ops
+// Exact conversions to double assembled with integer instructions, for kernels whose other work
+// has no FP64 instruction (GB300's FP64 pipe is a small fraction of its FP32 rate).
+// d >= 0: the double of an int32 distance
+__device__ __forceinline__ double nonneg_int_to_double(int d) {
+    if (d <= 0) return 0.0;
+    const int e = 31 - __clz(d);
+    const unsigned long long mant = ((unsigned long long)(unsigned)d << (52 - e)) & ((1ull << 52) - 1ull);
+    return __longlong_as_double((long long)(((unsigned long long)(1023 + e) << 52) | mant));
+}
+// the double of a float (every float exactly: zero, subnormal, normal, inf and nan)
+__device__ __forceinline__ double float_to_double(float x) {
+    const unsigned u = __float_as_uint(x);
+    const unsigned ex = (u >> 23) & 0xffu, mant = u & 0x7fffffu;
+    const unsigned long long sign = (unsigned long long)(u >> 31) << 63;
+    unsigned long long e, m;
+    if (ex == 0u) {
+        if (mant == 0u) return __longlong_as_double((long long)sign);
+        const int t = 31 - __clz(mant);  // subnormal: mant * 2^-149, leading bit t
+        e = (unsigned long long)(t + 874);
+        m = ((unsigned long long)mant << (52 - t)) & ((1ull << 52) - 1ull);
+    } else {
+        e = ex == 0xffu ? 0x7ffull : (unsigned long long)(ex + 896u);  // rebias 127 -> 1023
+        m = (unsigned long long)mant << 29;
+    }
+    return __longlong_as_double((long long)(sign | (e << 52) | m));
+}
+
 // ------------------------------------------------------------------------- precision
 struct PrecF64 {
     using D = double;
@@ -150,6 +178,7 @@ struct PrecF64 {
     __device__ static D store(const Acc& a) { return a.s; }
     __device__ static Acc load(D d) { return {d}; }
     __device__ static double value(const Acc& a) { return a.s; }
+    __device__ static void red_add(double* p, const Acc& a) { atomicAdd(p, a.s); }
 };
 
 struct PrecDF32 {
@@ -226,6 +255,11 @@ struct PrecDF32 {
     __device__ static D store(const Acc& a) { return make_float2(a.hi, a.lo); }
     __device__ static Acc load(D d) { return {d.x, d.y}; }
     __device__ static double value(const Acc& a) { return (double)a.hi + (double)a.lo; }
+    // BC[o] += value: the halves widened by integer ops (the same doubles as a conversion), one
+    // FP64 add and one FP64 reduction
+    __device__ static void red_add(double* p, const Acc& a) {
+        atomicAdd(p, float_to_double(a.hi) + float_to_double(a.lo));
+    }
 };
 
 // ------------------------------------------------------------------------ warp helpers
