@@ -79,6 +79,9 @@ struct KParams {
     const Unit* units;
     int64_t nunits;
     double* bc;                  // BC accumulator (FP64)
+    double* bc_seg;              // frontier kernel, one-segment launches: the accumulator in the
+                                 // segment's own vertex order, filled by the restore sweep (null:
+                                 // the dependency pass adds into bc through gid)
     double* bdist;               // border distances (0 when unreached)
     unsigned long long* bsig;    // border path counts
     unsigned long long* next_unit;

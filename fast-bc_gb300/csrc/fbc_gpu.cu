@@ -102,6 +102,7 @@ struct Options {
     int64_t wide_threads = 1024;       // block size of the wide frontier kernel (<= 1024)
     int64_t wide_kv = 1;               // level entries per lane of the 1024-thread form (1 or 2)
     int64_t adj4 = 1;                  // use the packed 4-byte adjacency where it exists
+    int64_t bc_sweep = 1;              // one-segment, one-source-per-block launches add BC in the restore sweep
     int64_t debug_sched = FBC_SCHED_PLAIN;  // schedule used by fbc_sssp_debug
     int64_t scratch_keep_mb = 8192;  // per-call scratch the memory pool keeps for later calls
 };
@@ -125,7 +126,7 @@ struct Ctx {
     cudaMemPool_t pool = nullptr;  // per-call scratch (TmpBuf), stream-ordered on st
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, evm = nullptr;
     Options opt;
-    DBuf retry, segs, units_b, units_w, chunks, crp, cadj, cgid, cbord, bc, bdist, bsig, ctr, dbg;
+    DBuf retry, segs, units_b, units_w, chunks, crp, cadj, cgid, cbord, bc, bdist, bsig, ctr, dbg, bcseg;
     // cluster extraction scratch: offsets, ids, flags, scans, given borders, error word
     DBuf c_off, c_id, c_lid, c_isb, c_flag, c_scan, c_sums, c_boff, c_bsrc, c_m, c_err;
     Workspace wsb, wsw;
@@ -625,8 +626,32 @@ int launch_block(const Plan& P, const std::vector<Unit>& units_in, int ws_n, fbc
     K.ws = W.buf.as<char>();
     K.ws_stride = W.stride;
     K.ws_n = (int32_t)W.ws_n;  // block kernel: vertices; frontier kernel: entries (v*K + k)
+    // one source per block, one segment: the restore sweep accumulates BC in the segment's order,
+    // coalesced (directly into bc without a map; through a segment-order buffer and one scatter
+    // afterwards with one), instead of a scattered reduction per vertex in the dependency pass
+    const Seg* one = nullptr;
+    if (c.fr && c.K == 1 && g.opt.bc_sweep) {
+        one = &P.segs[c.units[0].seg];
+        for (const Unit& u : c.units)
+            if (u.seg != c.units[0].seg) { one = nullptr; break; }
+    }
+    if (one) {
+        if (one->gid) {
+            FBC_CK(g.bcseg.ensure(sizeof(double) * (size_t)one->n));
+            FBC_CK(cudaMemsetAsync(g.bcseg.p, 0, sizeof(double) * (size_t)one->n, g.st));
+            K.bc_seg = g.bcseg.as<double>();
+        } else {
+            K.bc_seg = K.bc + one->out_base;
+        }
+    }
     c.kern<<<(unsigned)c.slots, c.threads, 0, g.st>>>(K);
     FBC_CK(cudaGetLastError());
+    if (one && one->gid) {
+        const unsigned gb = (unsigned)std::max<int64_t>(1, std::min<int64_t>((one->n + 255) / 256, 8192));
+        fbc::add_seg_kernel<<<gb, 256, 0, g.st>>>(K.bc_seg, one->gid, one->out_base, one->n, K.bc);
+        FBC_CK(cudaGetLastError());
+        ++launches;
+    }
     ++launches;
     if (st) {
         st->slots = (int32_t)c.slots;
@@ -1429,6 +1454,7 @@ int fbc_set_option(const char* key, int64_t value) {
     else if (k == "wide_threads") g.opt.wide_threads = std::max<int64_t>(64, std::min<int64_t>(1024, value / 32 * 32));
     else if (k == "wide_kv") g.opt.wide_kv = value <= 1 ? 1 : 2;
     else if (k == "adj4") g.opt.adj4 = value != 0;
+    else if (k == "bc_sweep") g.opt.bc_sweep = value != 0;
     else if (k == "group") {
         if (value != 0 && value != 1 && value != 2 && value != 4) return fail(FBC_ERR_INVALID_ARG, "group must be 0, 1, 2 or 4");
         g.opt.group = value;
@@ -1463,6 +1489,7 @@ int fbc_get_option(const char* key, int64_t* value) {
     else if (k == "wide_threads") *value = g.opt.wide_threads;
     else if (k == "wide_kv") *value = g.opt.wide_kv;
     else if (k == "adj4") *value = g.opt.adj4;
+    else if (k == "bc_sweep") *value = g.opt.bc_sweep;
     else if (k == "debug_sched") *value = g.opt.debug_sched;
     else if (k == "scratch_keep_mb") *value = g.opt.scratch_keep_mb;
     else return fail(FBC_ERR_INVALID_ARG, "unknown option " + k);

@@ -574,7 +574,7 @@ __device__ void frontier_group(const KParams& P, const Unit* us, const FState<Pr
                         }
                     }
                     S.rec[o[j].v].dlt = Prec::store(acc[j]);
-                    if (v != us[k].src) {
+                    if (v != us[k].src && !P.bc_seg) {
                         const double card = us[k].card;
                         const int64_t ov = sg.out_base + (sg.gid ? sg.gid[v] : v);
                         atomicAdd(P.bc + ov, card == 1.0 ? Prec::value(acc[j]) : card * Prec::value(acc[j]));
@@ -601,10 +601,26 @@ __device__ void frontier_group(const KParams& P, const Unit* us, const FState<Pr
         }
     }
     __syncthreads();
-    // restore: word = (inf, 0), sigma/counter = 0
-    for (int i = tid; i < nK; i += nth) {
-        S.word[i] = (unsigned long long)(unsigned)kInf << 32;
-        S.rec[i].sc = 0ull;
+    // restore: word = (inf, 0), sigma/counter = 0.  With a segment-order accumulator this sweep
+    // also adds card * delta of every reached vertex but the source, coalesced, instead of the
+    // dependency pass's scattered reductions through gid (the host adds it into bc at the end).
+    if (P.bc_seg && !bad) {
+        for (int i = tid; i < nK; i += nth) {
+            const int k = i & (K - 1);
+            const int v = i >> kSh;
+            if (dist_of(ldcg64(S.word + i)) != kInf && v != us[k].src && us[k].src >= 0) {
+                const double d = Prec::value(Prec::load(S.rec[i].dlt));
+                const double card = us[k].card;
+                atomicAdd(P.bc_seg + v, card == 1.0 ? d : card * d);
+            }
+            S.word[i] = (unsigned long long)(unsigned)kInf << 32;
+            S.rec[i].sc = 0ull;
+        }
+    } else {
+        for (int i = tid; i < nK; i += nth) {
+            S.word[i] = (unsigned long long)(unsigned)kInf << 32;
+            S.rec[i].sc = 0ull;
+        }
     }
     __syncthreads();
 }
@@ -640,6 +656,14 @@ __global__ void __launch_bounds__(kForm >= 2 ? 1024 : kForm == 1 ? 512 : 128, kF
         if (gi >= P.nunits) break;
         frontier_group<Prec, kForm == 3 ? 1 : 2, K, 1, kA4>(P, us, S, C, cap);
     }
+}
+
+// bc[out_base + gid[v]] += acc[v]: a one-segment launch's accumulator (segment order) added into
+// the output (gid injective, so plain read-modify-writes suffice on the launch's stream).
+__global__ void add_seg_kernel(const double* __restrict__ acc, const int32_t* __restrict__ gid, int64_t out_base,
+                               int n, double* bc) {
+    for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x)
+        bc[out_base + gid[v]] += acc[v];
 }
 
 }  // namespace fbc

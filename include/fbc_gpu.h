@@ -90,6 +90,8 @@ const char* fbc_last_error_string(void);
  *   "wide_threads"     block size of the wide frontier blocks (64..1024, a multiple of 32; above 512
  *                      a 1024-thread form with 64 registers per thread; default 1024)
  *   "wide_kv"          level entries per lane of the 1024-thread form: 1 (default) or 2
+ *   "bc_sweep"         1 (default): a one-segment launch of one source per block adds BC in its
+ *                      restore sweep (coalesced, segment order); 0: in the dependency pass
  *   "adj4"             1 (default): wide one-source blocks on a relabelled graph with fewer than 2^24
  *                      vertices and weights below 256 read its adjacency packed in 4 bytes; 0: 8 bytes
  *   "warp_max_n"       largest segment run warp-per-source in shared memory
