@@ -49,6 +49,8 @@ struct Seg {
     const int32_t* gid;     // n local -> output ids; BC index = out_base + (gid ? gid[v] : v)
     const int32_t* border;  // nb local ids of the border vertices (ascending global id)
     const uint32_t* adj4;   // the same adjacency packed as (destination | weight << 24), or null
+    const uint8_t* revw;    // weight of each edge's reverse (every edge has one, weights < 256),
+                            // or null: the frontier kernel then counts tight in-edges without atomics
     int64_t out_base;
     int32_t n;              // vertices
     int32_t nb;             // border vertices (cluster segments), else 0

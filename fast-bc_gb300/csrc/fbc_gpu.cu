@@ -103,6 +103,7 @@ struct Options {
     int64_t wide_kv = 1;               // level entries per lane of the 1024-thread form (1 or 2)
     int64_t adj4 = 1;                  // use the packed 4-byte adjacency where it exists
     int64_t bc_sweep = 1;              // one-segment, one-source-per-block launches add BC in the restore sweep
+    int64_t pull_count = 1;            // count tight in-edges by pulling over reverse weights where they exist
     int64_t debug_sched = FBC_SCHED_PLAIN;  // schedule used by fbc_sssp_debug
     int64_t scratch_keep_mb = 8192;  // per-call scratch the memory pool keeps for later calls
 };
@@ -176,6 +177,8 @@ struct fbc_graph_s {
     int32_t* d_ord_rp = nullptr;
     int2* d_ord_adj = nullptr;
     uint32_t* d_ord_adj4 = nullptr;  // packed (destination | weight << 24) when n < 2^24, weights < 256
+    uint8_t* d_ord_revw = nullptr;   // weight of each relabelled edge's reverse, when every edge has one
+                                     // and weights are below 256
     int32_t* d_ord_inv = nullptr;
     std::vector<int32_t> ord_new;
 };
@@ -423,6 +426,28 @@ int ensure_order(fbc_graph_s* G) {
         FBC_CK(cudaMemcpyAsync(G->d_ord_adj4, adj4.data(), sizeof(uint32_t) * adj4.size(), cudaMemcpyHostToDevice,
                                g.st));
     }
+    // reverse weights: edge u -> x gets the weight of x -> u (rows are sorted by destination);
+    // a graph with an edge that has no reverse gets none
+    std::vector<uint8_t> revw;
+    if (n > 0 && G->maxw < 256) {
+        revw.resize(adj.size());
+        bool sym = true;
+        for (int32_t u = 0; u < n && sym; ++u)
+            for (int32_t k = rp32[u]; k < rp32[u + 1]; ++k) {
+                const int32_t x = adj[k].x;
+                const auto b = adj.begin() + rp32[x], en = adj.begin() + rp32[x + 1];
+                const auto it = std::lower_bound(b, en, u, [](const int2& a, int32_t v) { return a.x < v; });
+                if (it == en || it->x != u) {
+                    sym = false;
+                    break;
+                }
+                revw[(size_t)k] = (uint8_t)it->y;
+            }
+        if (sym) {
+            FBC_CK(cudaMalloc(&G->d_ord_revw, revw.size()));
+            FBC_CK(cudaMemcpyAsync(G->d_ord_revw, revw.data(), revw.size(), cudaMemcpyHostToDevice, g.st));
+        }
+    }
     FBC_CK(cudaStreamSynchronize(g.st));
     G->ord_new = std::move(nw);
     G->ord_built = true;
@@ -568,12 +593,11 @@ int block_config(const Plan& P, const std::vector<Unit>& units_in, int ws_n, boo
             KernFn f = frontier_variant<Prec>(wide, K, threads, a4);
             int b = 0;
             FBC_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, f, threads, 0));
-            b = std::max(b, 1);
+            const int64_t full = (int64_t)g.nsm * std::max(b, 1);  // units resident at once
             const int64_t sb = fbc::fstate_bytes<Prec>((int64_t)ws_n * K);
             const int64_t strd = 256 + ((sb + 255) & ~int64_t(255));
             std::vector<Unit> gu = K > 1 ? group_units(sorted, K) : sorted;
             const int64_t groups = (int64_t)gu.size() / K;
-            const int64_t full = (int64_t)g.nsm * b;
             const int64_t sl = std::max<int64_t>(1, std::min<int64_t>(std::min(full, groups), budget / strd));
             const bool ok = K == 1 || forced > 0 || (groups >= full && sl >= full);
             if (!ok) continue;
@@ -602,6 +626,12 @@ int block_config(const Plan& P, const std::vector<Unit>& units_in, int ws_n, boo
     }
     if (!c.kern) return fail(FBC_ERR_INVALID_ARG, "no frontier kernel variant fits this segment");
     return FBC_OK;
+}
+
+// The launch of a block configuration: one block per slot.
+cudaError_t launch_units(const BlockCfg& c, const KParams& K, cudaStream_t st) {
+    c.kern<<<(unsigned)c.slots, c.threads, 0, st>>>(K);
+    return cudaGetLastError();
 }
 
 // Block-per-source launch on the library's workspace.
@@ -644,8 +674,7 @@ int launch_block(const Plan& P, const std::vector<Unit>& units_in, int ws_n, fbc
             K.bc_seg = K.bc + one->out_base;
         }
     }
-    c.kern<<<(unsigned)c.slots, c.threads, 0, g.st>>>(K);
-    FBC_CK(cudaGetLastError());
+    FBC_CK(launch_units(c, K, g.st));
     if (one && one->gid) {
         const unsigned gb = (unsigned)std::max<int64_t>(1, std::min<int64_t>((one->n + 255) / 256, 8192));
         fbc::add_seg_kernel<<<gb, 256, 0, g.st>>>(K.bc_seg, one->gid, one->out_base, one->n, K.bc);
@@ -1454,6 +1483,7 @@ int fbc_set_option(const char* key, int64_t value) {
     else if (k == "wide_threads") g.opt.wide_threads = std::max<int64_t>(64, std::min<int64_t>(1024, value / 32 * 32));
     else if (k == "wide_kv") g.opt.wide_kv = value <= 1 ? 1 : 2;
     else if (k == "adj4") g.opt.adj4 = value != 0;
+    else if (k == "pull_count") g.opt.pull_count = value != 0;
     else if (k == "bc_sweep") g.opt.bc_sweep = value != 0;
     else if (k == "group") {
         if (value != 0 && value != 1 && value != 2 && value != 4) return fail(FBC_ERR_INVALID_ARG, "group must be 0, 1, 2 or 4");
@@ -1490,6 +1520,7 @@ int fbc_get_option(const char* key, int64_t* value) {
     else if (k == "wide_kv") *value = g.opt.wide_kv;
     else if (k == "adj4") *value = g.opt.adj4;
     else if (k == "bc_sweep") *value = g.opt.bc_sweep;
+    else if (k == "pull_count") *value = g.opt.pull_count;
     else if (k == "debug_sched") *value = g.opt.debug_sched;
     else if (k == "scratch_keep_mb") *value = g.opt.scratch_keep_mb;
     else return fail(FBC_ERR_INVALID_ARG, "unknown option " + k);
@@ -1671,6 +1702,7 @@ int batched_graph_seg(fbc_graph_s* G, int64_t out_base, int sched, Seg& s, const
     s.rp = G->d_ord_rp;
     s.adj = G->d_ord_adj;
     s.adj4 = g.opt.adj4 ? G->d_ord_adj4 : nullptr;
+    s.revw = g.opt.pull_count ? G->d_ord_revw : nullptr;
     s.gid = G->d_ord_inv;
     map = G->ord_new.data();
     return FBC_OK;
@@ -1689,6 +1721,7 @@ int fbc_graph_free(fbc_graph G) {
     if (G->d_ord_rp) cudaFree(G->d_ord_rp);
     if (G->d_ord_adj) cudaFree(G->d_ord_adj);
     if (G->d_ord_adj4) cudaFree(G->d_ord_adj4);
+    if (G->d_ord_revw) cudaFree(G->d_ord_revw);
     if (G->d_ord_inv) cudaFree(G->d_ord_inv);
     delete G;
     return FBC_OK;
@@ -2173,7 +2206,7 @@ int plan_capture(fbc_plan_s* p, Plan& P) {
     if (ce != cudaSuccess) return fail(FBC_ERR_CUDA, std::string("capture: ") + cudaGetErrorString(ce));
     FBC_CK(cudaGraphInstantiate(&p->exec[0], p->graph[0], 0));
     FBC_CK(cudaStreamBeginCapture(g.st, cudaStreamCaptureModeThreadLocal));
-    if (!ub.empty()) bc.kern<<<(unsigned)bc.slots, bc.threads, 0, g.st>>>(K);
+    if (!ub.empty()) launch_units(bc, K, g.st);
     cudaMemcpyAsync(p->h_bc, p->bc.p, n8, cudaMemcpyDeviceToHost, g.st);
     if (p->ent > 0) {
         cudaMemcpyAsync(p->h_bdist, p->bdist.p, e8, cudaMemcpyDeviceToHost, g.st);

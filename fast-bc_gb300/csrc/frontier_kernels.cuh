@@ -336,16 +336,19 @@ __device__ void frontier_group(const KParams& P, const Unit* us, const FState<Pr
         // ------------------------------------------------------------- sigma (Kahn)
         // tight in-edge counts and each entry's tight out-edge mask: a sweep over all
         // entries, four per thread in flight; the K entries of a vertex sit on adjacent lanes,
-        // so their row and neighbour-word loads coalesce
+        // so their row and neighbour-word loads coalesce.  With reverse weights (pull) a vertex
+        // counts its own tight in-edges from the same neighbour words and stores its whole
+        // record at once; else each tight edge adds to its head's counter atomically.
+        const bool pull = sg.revw != nullptr;
         for (int v0 = tid; v0 < nK; v0 += 4 * nth) {
             int dv[4], e[4], e1[4], eb[4];
-            unsigned mk[4];
+            unsigned mk[4], cn[4];
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
                 const int vk = v0 + j * nth;
                 dv[j] = kInf;
                 e[j] = e1[j] = eb[j] = 0;
-                mk[j] = 0u;
+                mk[j] = cn[j] = 0u;
                 if (vk < nK) {
                     dv[j] = dist_of(ldcg64(S.word + vk));
                     if (dv[j] != kInf) {
@@ -355,15 +358,17 @@ __device__ void frontier_group(const KParams& P, const Unit* us, const FState<Pr
                 }
             }
             for (;;) {
-                int x[4], nd[4];
+                int x[4], nd[4], rw[4];
                 bool any = false;
 #pragma unroll
                 for (int j = 0; j < 4; ++j) {
                     x[j] = -1;
                     if (e[j] < e1[j]) {
-                        const int2 a = adj_at<kA4>(sg, e[j]++);
+                        const int ee = e[j]++;
+                        const int2 a = adj_at<kA4>(sg, ee);
                         x[j] = (a.x << kSh) + ((v0 + j * nth) & (K - 1));
                         nd[j] = dv[j] + a.y;
+                        rw[j] = pull ? (int)__ldg(sg.revw + ee) : 0;
                         any = true;
                     }
                 }
@@ -373,16 +378,25 @@ __device__ void frontier_group(const KParams& P, const Unit* us, const FState<Pr
                 for (int j = 0; j < 4; ++j) dx[j] = x[j] >= 0 ? dist_of(ldcg64(S.word + x[j])) : -1;
 #pragma unroll
                 for (int j = 0; j < 4; ++j)
-                    if (x[j] >= 0 && nd[j] == dx[j]) {
-                        atomicAdd(&S.rec[x[j]].sc, 1ull);
-                        const int bit = e[j] - 1 - eb[j];
-                        if (bit < 32) mk[j] |= 1u << bit;
+                    if (x[j] >= 0) {
+                        if (nd[j] == dx[j]) {
+                            if (!pull) atomicAdd(&S.rec[x[j]].sc, 1ull);
+                            const int bit = e[j] - 1 - eb[j];
+                            if (bit < 32) mk[j] |= 1u << bit;
+                        }
+                        if (pull && dx[j] != kInf && dx[j] + rw[j] == dv[j]) ++cn[j];  // x -> v is tight
                     }
             }
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
                 const int vk = v0 + j * nth;
-                if (vk < nK && dv[j] != kInf) S.rec[vk].mask = e1[j] - eb[j] > mask_edges ? 0xffffffffu : mk[j];
+                if (vk < nK && dv[j] != kInf) {
+                    const unsigned mv = e1[j] - eb[j] > mask_edges ? 0xffffffffu : mk[j];
+                    if (pull)  // count (sigma 0) and mask: the whole record, one 16-byte store
+                        *reinterpret_cast<ulonglong2*>(S.rec + vk) = make_ulonglong2(cn[j], mv);
+                    else
+                        S.rec[vk].mask = mv;
+                }
             }
         }
         __syncthreads();
@@ -614,7 +628,9 @@ __device__ void frontier_group(const KParams& P, const Unit* us, const FState<Pr
         }
     }
     __syncthreads();
-    // restore: word = (inf, 0), sigma/counter = 0.  With a segment-order accumulator this sweep
+    // restore: word = (inf, 0), sigma/counter = 0 (not with reverse weights: the counting sweep
+    // then stores every reached record whole, and the slot header records the extent left
+    // unclean for a later atomic-count unit).  With a segment-order accumulator this sweep
     // also adds card * delta of every reached vertex but the source, coalesced, instead of the
     // dependency pass's scattered reductions through gid (the host adds it into bc at the end).
     if (P.bc_seg && !bad) {
@@ -627,12 +643,12 @@ __device__ void frontier_group(const KParams& P, const Unit* us, const FState<Pr
                 atomicAdd(P.bc_seg + v, card == 1.0 ? d : card * d);
             }
             S.word[i] = (unsigned long long)(unsigned)kInf << 32;
-            S.rec[i].sc = 0ull;
+            if (!sg.revw) S.rec[i].sc = 0ull;
         }
     } else {
         for (int i = tid; i < nK; i += nth) {
             S.word[i] = (unsigned long long)(unsigned)kInf << 32;
-            S.rec[i].sc = 0ull;
+            if (!sg.revw) S.rec[i].sc = 0ull;
         }
     }
     __syncthreads();
@@ -667,7 +683,23 @@ __global__ void __launch_bounds__(kForm >= 2 ? 1024 : kForm == 1 ? 512 : 128, kF
         if (gi < P.nunits && threadIdx.x < K) us[threadIdx.x] = P.units[gi * K + threadIdx.x];
         __syncthreads();
         if (gi >= P.nunits) break;
+        // header word 1: entries whose counters a pull-count unit (reverse weights) left
+        // non-zero; an atomic-count unit clears them first
+        const Seg& sgu = P.segs[us[0].seg];
+        const bool pull = sgu.revw != nullptr;
+        if (!pull) {
+            const unsigned dirty = __ldcg(hdr + 1);
+            if (dirty) {
+                for (int64_t i = threadIdx.x; i < (int64_t)dirty; i += blockDim.x) S.rec[i].sc = 0ull;
+                __syncthreads();
+                if (threadIdx.x == 0) hdr[1] = 0u;
+            }
+        }
         frontier_group<Prec, kForm == 3 ? 1 : 2, K, 1, kA4>(P, us, S, C, cap);
+        if (pull && threadIdx.x == 0) {
+            const unsigned nk = (unsigned)sgu.n * (unsigned)K;
+            if (__ldcg(hdr + 1) < nk) hdr[1] = nk;
+        }
     }
 }
 

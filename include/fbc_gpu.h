@@ -94,6 +94,9 @@ const char* fbc_last_error_string(void);
  *                      restore sweep (coalesced, segment order); 0: in the dependency pass
  *   "adj4"             1 (default): wide one-source blocks on a relabelled graph with fewer than 2^24
  *                      vertices and weights below 256 read its adjacency packed in 4 bytes; 0: 8 bytes
+ *   "pull_count"       1 (default): on a relabelled graph whose every edge has a reverse (weights
+ *                      below 256) the frontier kernel counts each vertex's tight in-edges from its
+ *                      own row and the reverse weights, without atomics; 0: atomic counts
  *   "warp_max_n"       largest segment run warp-per-source in shared memory
  *   "order_min_n"      batched runs relabel graphs of at least this many vertices for memory
  *                      locality (outputs stay in input ids)

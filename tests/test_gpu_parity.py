@@ -422,3 +422,4 @@ def test_large_path_counts_are_recomputed_exactly(fg):
     b = fg.dependency_batch(g, src, None, fg.FP64, fg.PLAIN)
     assert rel_err(a, b) <= TOL_FP64
     assert rel_err(a, oracle.exact_bc_sources(og, src, threads=8)) <= TOL_FP64
+
