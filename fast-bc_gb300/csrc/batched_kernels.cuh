@@ -330,7 +330,7 @@ __device__ void small_unit(const KParams& K, const Seg& sg, const Unit& u, const
     if (!bad) {
         // --------------------------------------------------------- dependency
         const double card = u.card;
-        const bool card1 = card == 1.0;  // one FP64 compare per unit, not per vertex
+        const bool card1 = __double_as_longlong(card) == 0x3ff0000000000000ll;  // card == 1.0, bitwise
         for (int L = nlev - 1; L >= 0; --L) {
             const int a1 = lvl[L + 1];
             for (int i = lvl[L] + lane; i < a1; i += 32) {

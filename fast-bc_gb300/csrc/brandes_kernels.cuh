@@ -260,10 +260,12 @@ struct PrecDF32 {
     __device__ static D store(const Acc& a) { return make_float2(a.hi, a.lo); }
     __device__ static Acc load(D d) { return {d.x, d.y}; }
     __device__ static double value(const Acc& a) { return (double)a.hi + (double)a.lo; }
-    // BC[o] += value: the halves widened by integer ops (the same doubles as a conversion), one
-    // FP64 add and one FP64 reduction
+    // BC[o] += value: the halves widened by integer ops (the same doubles as a conversion) and
+    // reduced one after the other, so the cross-source sum is the only FP64 arithmetic, done by
+    // the reductions in L2 (the FP64 pipe stays idle)
     __device__ static void red_add(double* p, const Acc& a) {
-        atomicAdd(p, float_to_double(a.hi) + float_to_double(a.lo));
+        atomicAdd(p, float_to_double(a.hi));
+        if (a.lo != 0.f) atomicAdd(p, float_to_double(a.lo));
     }
 };
 

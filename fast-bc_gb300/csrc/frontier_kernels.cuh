@@ -7,9 +7,9 @@
 //   * one 64-bit word per vertex, (dist << 32 | stamp): a single global atomicMin both relaxes
 //     the edge and reports whether the vertex already sits in the queue the relaxation
 //     pushes it to (the queue's stamp), so there is no second atomic on a flag array;
-//   * queue and Kahn-level entries carry the vertex's row start (loaded from the small,
-//     L2-resident row offsets alongside the atomic that pushed it), so a step issues its
-//     adjacency loads with its first state load;
+//   * queue entries carry the vertex's row (loaded from the small, L2-resident row offsets
+//     alongside the atomic that pushed it) and Kahn-level entries carry distance, row, final
+//     path count and tight-edge mask, so a step starts with its adjacency loads;
 //   * path count and Kahn counter share one 64-bit word (sigma << B | counter; B = 8 bits when
 //     no vertex has 255 or more in-edges, else 16), so one atomic
 //     both adds sigma_v and retires the edge, and the thread that retires the last tight
@@ -30,13 +30,16 @@ namespace fbc {
 struct QEnt {
     int v, e0;
 };
-// A Kahn-level entry: the vertex entry and its row start.  The vertex's final path count and
-// tight-edge mask are read from its record when the entry is taken: the Kahn pass finds the
-// record in L2 (its release atomic just touched it) and the dependency pass needs the record's
-// sector anyway for the dependency it stores there, so 8-byte entries halve the level lists'
-// DRAM traffic at no extra sector.
+// A Kahn-level entry: row start and (final path count << B | tight-edge mask), B the launch's
+// field width (8 or 16 bits).  The mask is the vertex's tight out-edges found by the counting
+// sweep (bit k: edge e0 + k), so that the Kahn and dependency passes touch only those; all B
+// bits set (the long-row mark) for rows of B or more edges (then every edge of the row is
+// re-tested against the distances).  Path counts are below 2^(64 - B) here.  (Entries of 8 bytes,
+// the count and mask read from the vertex's record instead, measured 0.5% faster on the 4M-vertex
+// grid and 7% slower on graphs whose state stays in L2: one more dependent load per entry.)
 struct LEnt {
     int v, e0;
+    unsigned long long sigdm;
 };
 // the packed fields of one launch: B = cb bits of counter / mask next to the path count
 struct Packing {
@@ -45,10 +48,8 @@ struct Packing {
     unsigned long long sigmax;   // 2^(64 - cb) - 1
     __device__ explicit Packing(int bits)
         : cb(bits), low((1ull << bits) - 1ull), sigmax((1ull << (64 - bits)) - 1ull) {}
-    // the tight-edge mask as stored in a record: all ones for a long row, else up to B - 1 bits
-    __device__ unsigned mask_of(unsigned long long slot) const {
-        const unsigned m = (unsigned)slot;
-        return m == 0xffffffffu ? (unsigned)low : m;
+    __device__ unsigned long long sig_dm(unsigned long long sig, unsigned mask) const {
+        return (sig << cb) | (mask == 0xffffffffu ? low : ((unsigned long long)mask & low));
     }
 };
 
@@ -250,13 +251,15 @@ __device__ void frontier_group(const KParams& P, const Unit* us, const FState<Pr
                             r0[t] = __ldg(rp + a.x);  // x's row, in flight with the atomic
                         }
                     }
-                    // a relaxation that cannot lower the current distance is dropped after a plain
-                    // load (distances only fall, so a stale word can only overstate it): most
-                    // edges of a settled wavefront fail, and a random load costs the memory
-                    // system about half of what a random atomic does
+                    // on the large relabelled graphs (packed adjacency) a relaxation that cannot
+                    // lower the current distance is dropped after a plain load (distances only
+                    // fall, so a stale word can only overstate it): most edges of a settled
+                    // wavefront fail, and a scattered load costs the memory system about half of
+                    // what a scattered atomic does (1% there; on graphs whose state stays in L2 the
+                    // extra dependent load costs more than it saves)
 #pragma unroll
                     for (int t = 0; t < kE * 4; ++t)
-                        if (x[t] >= 0) old[t] = ldcg64(S.word + x[t]);
+                        old[t] = kA4 && x[t] >= 0 ? ldcg64(S.word + x[t]) : (unsigned long long)(unsigned)kInf << 32;
 #pragma unroll
                     for (int t = 0; t < kE * 4; ++t)
                         if (x[t] >= 0 && nd[t] < dist_of(old[t]))
@@ -405,8 +408,7 @@ __device__ void frontier_group(const KParams& P, const Unit* us, const FState<Pr
             for (int k = 0; k < K; ++k) {
                 const int src = us[k].src;
                 if (src < 0) continue;
-                S.rec[src * K + k].sc = 1ull << pk.cb;  // sigma_s = 1, no in-edges
-                S.order[c++] = LEnt{src * K + k, __ldg(rp + src)};
+                S.order[c++] = LEnt{src * K + k, __ldg(rp + src), pk.sig_dm(1ull, __ldcg(&S.rec[src * K + k].mask))};
             }
             S.lvl[0] = 0;
             C.ocnt = c;
@@ -431,10 +433,9 @@ __device__ void frontier_group(const KParams& P, const Unit* us, const FState<Pr
                     sv[j] = 0ull;
                     if (i < hi) {
                         const LEnt o = S.order[i];
-                        const ulonglong2 r = __ldcg(reinterpret_cast<const ulonglong2*>(S.rec + o.v));
-                        sv[j] = r.x >> pk.cb;
+                        sv[j] = o.sigdm >> pk.cb;
                         e0[j] = o.e0;
-                        mk[j] = pk.mask_of(r.y);
+                        mk[j] = (unsigned)(o.sigdm & pk.low);
                         kk[j] = o.v & (K - 1);
                         if (mk[j] == (unsigned)pk.low) {  // long row: walk it and re-test every edge
                             dv[j] = dist_of(ldcg64(S.word + o.v));
@@ -474,19 +475,25 @@ __device__ void frontier_group(const KParams& P, const Unit* us, const FState<Pr
                     for (int j = 0; j < kV; ++j)
                         if (x[j] >= 0 && !tight[j]) tight[j] = nd[j] == dist_of(ldcg64(S.word + x[j]));
                     unsigned long long old[kV];
+                    unsigned tm[kV];
 #pragma unroll
                     for (int j = 0; j < kV; ++j)
-                        if (tight[j])  // one atomic adds sigma_v and retires the edge
+                        if (tight[j]) {
+                            // one atomic adds sigma_v and retires the edge; the thread that
+                            // retires the last tight in-edge knows x's final count
                             old[j] = atomicAdd(&S.rec[x[j]].sc, (sv[j] << pk.cb) - 1ull);
+                            tm[j] = __ldcg(&S.rec[x[j]].mask);  // same sector as the atomic
+                        }
 #pragma unroll
                     for (int j = 0; j < kV; ++j) {
                         bool push = false;
-                        LEnt le{x[j], 0};
+                        LEnt le{x[j], 0, 0ull};
                         if (tight[j]) {
                             const unsigned long long sx = (old[j] >> pk.cb) + sv[j];
                             if (sx > pk.sigmax || sv[j] > pk.sigmax) bad |= kErrRetry;
-                            push = (old[j] & pk.low) == 1ull;  // the last tight in-edge: x is final
+                            push = (old[j] & pk.low) == 1ull;
                             le.e0 = r0[j];
+                            le.sigdm = pk.sig_dm(sx, tm[j]);
                         }
                         bpush(push, le, S.order, &C.ocnt, (int)cap + 1, &C.ovf);
                     }
@@ -526,8 +533,6 @@ __device__ void frontier_group(const KParams& P, const Unit* us, const FState<Pr
             for (int base = a0 + (tid & ~31) * kV; base < a1; base += nth * kV) {
                 LEnt o[kV];
                 unsigned mk[kV];
-                unsigned long long svs[kV];
-                bool lr[kV];
                 typename Prec::Acc acc[kV];
 #pragma unroll
                 for (int j = 0; j < kV; ++j) {
@@ -535,17 +540,10 @@ __device__ void frontier_group(const KParams& P, const Unit* us, const FState<Pr
                     acc[j] = Prec::zero();
                     o[j].v = -1;
                     mk[j] = 0u;
-                    svs[j] = 0ull;
-                    lr[j] = false;
                     if (i < a1) {
                         o[j] = S.order[i];
-                        // the vertex's own record: final count and mask (its dependency goes
-                        // into the same sector below)
-                        const ulonglong2 r = __ldcg(reinterpret_cast<const ulonglong2*>(S.rec + o[j].v));
-                        svs[j] = r.x >> pk.cb;
-                        mk[j] = pk.mask_of(r.y);
-                        lr[j] = mk[j] == (unsigned)pk.low;
-                        if (lr[j]) mk[j] = 0u;
+                        mk[j] = (unsigned)(o[j].sigdm & pk.low);
+                        if (mk[j] == (unsigned)pk.low) mk[j] = 0u;
                     }
                 }
                 for (;;) {
@@ -575,7 +573,7 @@ __device__ void frontier_group(const KParams& P, const Unit* us, const FState<Pr
 #pragma unroll
                     for (int j = 0; j < kV; ++j)
                         if (x[j] >= 0) {
-                            const unsigned long long sv = svs[j];
+                            const unsigned long long sv = o[j].sigdm >> pk.cb;
                             if (sx[j] == sv) Prec::add_same(acc[j], dx[j]);
                             else Prec::add(acc[j], sv, sx[j], dx[j]);
                         }
@@ -584,10 +582,10 @@ __device__ void frontier_group(const KParams& P, const Unit* us, const FState<Pr
                 for (int j = 0; j < kV; ++j) {
                     if (o[j].v < 0) continue;
                     const int v = o[j].v >> kSh, k = o[j].v & (K - 1);
-                    if (lr[j]) {  // long row: re-test every edge
+                    if ((o[j].sigdm & pk.low) == pk.low) {  // long row: re-test every edge
                         const int e1 = __ldg(rp + v + 1);
                         const int dv = dist_of(ldcg64(S.word + o[j].v));
-                        const unsigned long long sv = svs[j];
+                        const unsigned long long sv = o[j].sigdm >> pk.cb;
                         for (int e = o[j].e0; e < e1; ++e) {
                             const int2 a = adj_at<kA4>(sg, e);
                             const int xk = (a.x << kSh) + k;
