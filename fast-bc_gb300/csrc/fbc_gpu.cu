@@ -104,6 +104,7 @@ struct Options {
     int64_t adj4 = 1;                  // use the packed 4-byte adjacency where it exists
     int64_t bc_sweep = 1;              // one-segment, one-source-per-block launches add BC in the restore sweep
     int64_t pull_count = 1;            // count tight in-edges by pulling over reverse weights where they exist
+    int64_t source_order = 1;          // batched sources of a relabelled graph run in its locality order
     int64_t debug_sched = FBC_SCHED_PLAIN;  // schedule used by fbc_sssp_debug
     int64_t scratch_keep_mb = 8192;  // per-call scratch the memory pool keeps for later calls
 };
@@ -1484,6 +1485,7 @@ int fbc_set_option(const char* key, int64_t value) {
     else if (k == "wide_kv") g.opt.wide_kv = value <= 1 ? 1 : 2;
     else if (k == "adj4") g.opt.adj4 = value != 0;
     else if (k == "pull_count") g.opt.pull_count = value != 0;
+    else if (k == "source_order") g.opt.source_order = value != 0;
     else if (k == "bc_sweep") g.opt.bc_sweep = value != 0;
     else if (k == "group") {
         if (value != 0 && value != 1 && value != 2 && value != 4) return fail(FBC_ERR_INVALID_ARG, "group must be 0, 1, 2 or 4");
@@ -1521,6 +1523,7 @@ int fbc_get_option(const char* key, int64_t* value) {
     else if (k == "adj4") *value = g.opt.adj4;
     else if (k == "bc_sweep") *value = g.opt.bc_sweep;
     else if (k == "pull_count") *value = g.opt.pull_count;
+    else if (k == "source_order") *value = g.opt.source_order;
     else if (k == "debug_sched") *value = g.opt.debug_sched;
     else if (k == "scratch_keep_mb") *value = g.opt.scratch_keep_mb;
     else return fail(FBC_ERR_INVALID_ARG, "unknown option " + k);
@@ -1778,6 +1781,10 @@ int fbc_sssp_dependency_batch(fbc_graph G, int64_t count, const int32_t* sources
     P.seg_maxindeg.push_back(G->maxindeg);
     for (int64_t i = 0; i < count; ++i)
         P.units.push_back(Unit{0, map ? map[sources[i]] : sources[i], cards ? cards[i] : 1.0, -1});
+    // on a relabelled graph, sources in the locality order: the sources running at once then
+    // start near each other, and their wavefronts read the same rows at about the same time
+    if (map && g.opt.source_order)
+        std::stable_sort(P.units.begin(), P.units.end(), [](const Unit& a, const Unit& b) { return a.src < b.src; });
     P.bc_len = G->n;
     if (st) st->h2d_bytes += count * (int64_t)(sizeof(int32_t) + sizeof(double));
     FBC_TRY(run_plan(P, st));
