@@ -97,6 +97,8 @@ const char* fbc_last_error_string(void);
  *   "pull_count"       1 (default): on a relabelled graph whose every edge has a reverse (weights
  *                      below 256) the frontier kernel counts each vertex's tight in-edges from its
  *                      own row and the reverse weights, without atomics; 0: atomic counts
+ *   "source_order"     1 (default): the sources of a batched call on a relabelled graph run in its
+ *                      locality order (sources running at once start near each other); 0: as given
  *   "warp_max_n"       largest segment run warp-per-source in shared memory
  *   "order_min_n"      batched runs relabel graphs of at least this many vertices for memory
  *                      locality (outputs stay in input ids)
