@@ -97,7 +97,7 @@ struct Options {
     int64_t iter_mult = 16;
     int64_t ws_budget_mb = 0;   // 0 = 60% of the free device memory
     int64_t group = 0;          // frontier kernel sources per block (1, 2, 4); 0 = automatic
-    int64_t order_min_n = 131072;  // batched runs relabel graphs of at least this many vertices
+    int64_t order_min_n = 65536;   // batched runs relabel graphs of at least this many vertices
     int64_t csr_device_min_m = 65536;  // edge lists of at least this many edges are built on the device
     int64_t wide_threads = 1024;       // block size of the wide frontier kernel (<= 1024)
     int64_t wide_kv = 1;               // level entries per lane of the 1024-thread form (1 or 2)
