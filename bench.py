@@ -645,6 +645,7 @@ def run_extra(args):
     launches = 0
     kern = {"warp_ms": 0.0, "block_ms": 0.0, "warp_bytes": 0.0, "block_bytes": 0.0}
     phases = {}
+    clocks = Clocks(0)
     for _ in range(args.steps):
         flush.zero_()
         torch.cuda.synchronize()
@@ -659,15 +660,19 @@ def run_extra(args):
             ph[1] += st.relaxations
             for k in kern:
                 kern[k] += getattr(st, k)
+    clk = clocks.stop()
     dom = "warp" if kern["warp_ms"] >= kern["block_ms"] else "block"
     achieved = kern[f"{dom}_bytes"] / (kern[f"{dom}_ms"] / 1e3) / 1e9 if kern[f"{dom}_ms"] else 0.0
+    peak, peak_src = peak_hbm()
     line = {"metric": METRIC, "value": wl.work * args.steps / dev / 1e9, "unit": "GTEPS", "n_gpus": 1,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev / args.steps * 1e3,
             "higher_is_better": True, "dtype": "f32x2+u64" if prec == fg.FP32C else "f64+u64",
             "config": dict(wl.config, precision=args.prec, schedule=args.sched, autotuned=tuned),
             "e2e": {"value": wl.work * args.steps / wall / 1e9, "unit": "GTEPS"},
             "gpu_launches": launches,
-            "roofline": {"kernel": dom, "achieved": achieved, "unit": "GB/s"}}
+            "roofline": {"kernel": dom, "achieved": achieved, "unit": "GB/s", "peak": peak,
+                         "frac": achieved / peak if peak else None, "peak_source": peak_src},
+            "clocks": clk}
     if len(phases) > 1:
         line["phases"] = [{"device_ms_per_step": ms / args.steps, "gteps": rel / ms / 1e6 if ms else None}
                           for ms, rel in (phases[i] for i in sorted(phases))]
