@@ -9,6 +9,8 @@
 #include <cstdio>
 #include <cstring>
 #include <memory>
+#include <atomic>
+#include <condition_variable>
 #include <mutex>
 #include <numeric>
 #include <string>
@@ -320,29 +322,51 @@ struct Plan {
     double* dbg_dlt = nullptr;
 };
 
+// fn(lo, hi) over [0, count) in contiguous chunks on the host's threads (one chunk when small).
+template <class F>
+void host_parallel(int64_t count, F&& fn) {
+    const int nthr = (int)std::min<unsigned>(std::max(1u, std::thread::hardware_concurrency()), 32u);
+    if (nthr <= 1 || count < 65536) {
+        fn((int64_t)0, count);
+        return;
+    }
+    const int64_t chunk = (count + nthr - 1) / nthr;
+    std::vector<std::thread> th;
+    for (int i = 0; i < nthr; ++i) {
+        const int64_t lo = (int64_t)i * chunk, hi = std::min<int64_t>(count, lo + chunk);
+        if (lo >= hi) break;
+        th.emplace_back([&fn, lo, hi] { fn(lo, hi); });
+    }
+    for (auto& x : th) x.join();
+}
+
 // Recursive BFS bisection: a part (a range of `ord`) is laid out in the order of a BFS from its
 // first vertex that stays inside the part (vertices it cannot reach follow in their current
 // order), then halved; parts of at most `leaf` vertices are sorted by id.  Neighbours end up
 // close together at every scale, so a wavefront's vertices share sectors and DRAM pages.
 std::vector<int32_t> bisection_order(int32_t n, const std::vector<int64_t>& rp, const std::vector<int32_t>& col,
                                      int leaf) {
-    std::vector<int32_t> ord((size_t)n), tmp((size_t)n), part((size_t)n, 0);
+    std::vector<int32_t> ord((size_t)n), tmp((size_t)n);
+    std::unique_ptr<std::atomic<int32_t>[]> part(new std::atomic<int32_t>[(size_t)std::max(n, 1)]);
     std::vector<char> vis((size_t)n, 0);
-    for (int32_t i = 0; i < n; ++i) ord[i] = i;
-    std::vector<std::pair<int64_t, int64_t>> stk;
-    stk.emplace_back(0, n);
-    int32_t pid = 1;
-    while (!stk.empty()) {
-        const auto [lo, hi] = stk.back();
-        stk.pop_back();
+    for (int32_t i = 0; i < n; ++i) {
+        ord[i] = i;
+        part[i].store(0, std::memory_order_relaxed);
+    }
+    std::atomic<int32_t> pid{1};
+    // One range [lo, hi) of the current order: lay it out in BFS order (from each not yet reached
+    // vertex in turn, edges followed only inside the range), or sort a leaf.  Ranges processed at
+    // the same time are disjoint, so they touch disjoint vertices; a neighbour outside the range
+    // carries another range's id (ids are never reused), read and written atomically.
+    auto split = [&](int64_t lo, int64_t hi) -> bool {
         const int64_t len = hi - lo;
         if (len <= leaf) {
             std::sort(ord.begin() + lo, ord.begin() + hi);
-            continue;
+            return false;
         }
-        const int32_t me = pid++;
-        for (int64_t i = lo; i < hi; ++i) part[ord[i]] = me;
-        int64_t qt = 0;
+        const int32_t me = pid.fetch_add(1, std::memory_order_relaxed);
+        for (int64_t i = lo; i < hi; ++i) part[ord[i]].store(me, std::memory_order_relaxed);
+        int64_t qt = lo;
         for (int64_t i = lo; i < hi; ++i) {
             const int32_t s0 = ord[i];
             if (vis[s0]) continue;
@@ -353,20 +377,72 @@ std::vector<int32_t> bisection_order(int32_t n, const std::vector<int64_t>& rp, 
                 const int32_t v = tmp[qh++];
                 for (int64_t e = rp[v]; e < rp[v + 1]; ++e) {
                     const int32_t x = col[e];
-                    if (part[x] == me && !vis[x]) {
+                    if (part[x].load(std::memory_order_relaxed) == me && !vis[x]) {
                         vis[x] = 1;
                         tmp[qt++] = x;
                     }
                 }
             }
         }
-        for (int64_t i = 0; i < len; ++i) {
-            ord[lo + i] = tmp[i];
+        for (int64_t i = lo; i < hi; ++i) {
+            ord[i] = tmp[i];
             vis[tmp[i]] = 0;
         }
-        const int64_t mid = lo + len / 2;
-        stk.emplace_back(mid, hi);
-        stk.emplace_back(lo, mid);
+        return true;
+    };
+    // a range and everything below it, in this thread
+    auto serial = [&](int64_t lo0, int64_t hi0) {
+        std::vector<std::pair<int64_t, int64_t>> stk{{lo0, hi0}};
+        while (!stk.empty()) {
+            const auto [lo, hi] = stk.back();
+            stk.pop_back();
+            if (!split(lo, hi)) continue;
+            const int64_t mid = lo + (hi - lo) / 2;
+            stk.emplace_back(mid, hi);
+            stk.emplace_back(lo, mid);
+        }
+    };
+    // the top of the tree on a pool of host threads (the result does not depend on their number
+    // or timing: each range's layout depends only on its own order and the graph)
+    const int nthr = (int)std::min<unsigned>(std::max(1u, std::thread::hardware_concurrency()), 32u);
+    constexpr int64_t kSerial = 65536;
+    if (nthr <= 1 || n <= kSerial) {
+        serial(0, n);
+    } else {
+        std::mutex mu;
+        std::condition_variable cv;
+        std::vector<std::pair<int64_t, int64_t>> q{{0, (int64_t)n}};
+        int64_t pending = 1;  // ranges queued or in progress
+        auto work = [&]() {
+            for (;;) {
+                std::pair<int64_t, int64_t> r;
+                {
+                    std::unique_lock<std::mutex> lk(mu);
+                    cv.wait(lk, [&] { return !q.empty() || pending == 0; });
+                    if (q.empty()) return;  // pending == 0: everything is done
+                    r = q.back();
+                    q.pop_back();
+                }
+                bool done_here = true;
+                if (r.second - r.first <= kSerial) {
+                    serial(r.first, r.second);
+                } else if (split(r.first, r.second)) {
+                    const int64_t mid = r.first + (r.second - r.first) / 2;
+                    std::lock_guard<std::mutex> lk(mu);
+                    q.emplace_back(mid, r.second);
+                    q.emplace_back(r.first, mid);
+                    pending += 2;
+                    done_here = false;
+                }
+                std::lock_guard<std::mutex> lk(mu);
+                --pending;
+                if (!done_here) cv.notify_all();
+                else if (pending == 0) cv.notify_all();
+            }
+        };
+        std::vector<std::thread> th;
+        for (int i = 0; i < nthr; ++i) th.emplace_back(work);
+        for (auto& x : th) x.join();
     }
     std::vector<int32_t> nw((size_t)n);
     for (int32_t i = 0; i < n; ++i) nw[ord[i]] = i;
@@ -401,18 +477,22 @@ int ensure_order(fbc_graph_s* G) {
     const int32_t n = G->n;
     std::vector<int32_t> nw = bisection_order(n, G->h_rp, G->h_col, 16);
     std::vector<int32_t> inv((size_t)std::max(n, 1));
-    for (int32_t v = 0; v < n; ++v) inv[nw[v]] = v;
+    host_parallel(n, [&](int64_t lo, int64_t hi) {
+        for (int64_t v = lo; v < hi; ++v) inv[nw[v]] = (int32_t)v;
+    });
+    // the relabelled rows: offsets by a scan of the degrees in the new order, then each row filled
+    // and sorted by destination on its own
     std::vector<int32_t> rp32((size_t)n + 1, 0);
+    for (int32_t u = 0; u < n; ++u) rp32[u + 1] = rp32[u] + (int32_t)(G->h_rp[inv[u] + 1] - G->h_rp[inv[u]]);
     std::vector<int2> adj((size_t)std::max<int64_t>(G->m, 1));
-    int64_t e = 0;
-    for (int32_t u = 0; u < n; ++u) {
-        const int32_t v = inv[u];
-        rp32[u] = (int32_t)e;
-        const int64_t b = e;
-        for (int64_t k = G->h_rp[v]; k < G->h_rp[v + 1]; ++k) adj[e++] = make_int2(nw[G->h_col[k]], G->h_w[k]);
-        std::sort(adj.begin() + b, adj.begin() + e, [](const int2& a, const int2& c) { return a.x < c.x; });
-    }
-    rp32[n] = (int32_t)e;
+    host_parallel(n, [&](int64_t lo, int64_t hi) {
+        for (int64_t u = lo; u < hi; ++u) {
+            const int32_t v = inv[u];
+            int64_t e = rp32[u];
+            for (int64_t k = G->h_rp[v]; k < G->h_rp[v + 1]; ++k) adj[e++] = make_int2(nw[G->h_col[k]], G->h_w[k]);
+            std::sort(adj.begin() + rp32[u], adj.begin() + e, [](const int2& a, const int2& c) { return a.x < c.x; });
+        }
+    });
     FBC_CK(cudaMalloc(&G->d_ord_rp, sizeof(int32_t) * rp32.size()));
     FBC_CK(cudaMalloc(&G->d_ord_adj, sizeof(int2) * adj.size()));
     FBC_CK(cudaMalloc(&G->d_ord_inv, sizeof(int32_t) * inv.size()));
@@ -422,7 +502,9 @@ int ensure_order(fbc_graph_s* G) {
     std::vector<uint32_t> adj4;
     if (n < (1 << 24) && G->maxw < 256) {
         adj4.resize(adj.size());
-        for (size_t k = 0; k < adj.size(); ++k) adj4[k] = (uint32_t)adj[k].x | ((uint32_t)adj[k].y << 24);
+        host_parallel((int64_t)adj.size(), [&](int64_t lo, int64_t hi) {
+            for (int64_t k = lo; k < hi; ++k) adj4[k] = (uint32_t)adj[k].x | ((uint32_t)adj[k].y << 24);
+        });
         FBC_CK(cudaMalloc(&G->d_ord_adj4, sizeof(uint32_t) * adj4.size()));
         FBC_CK(cudaMemcpyAsync(G->d_ord_adj4, adj4.data(), sizeof(uint32_t) * adj4.size(), cudaMemcpyHostToDevice,
                                g.st));
@@ -432,19 +514,21 @@ int ensure_order(fbc_graph_s* G) {
     std::vector<uint8_t> revw;
     if (n > 0 && G->maxw < 256) {
         revw.resize(adj.size());
-        bool sym = true;
-        for (int32_t u = 0; u < n && sym; ++u)
-            for (int32_t k = rp32[u]; k < rp32[u + 1]; ++k) {
-                const int32_t x = adj[k].x;
-                const auto b = adj.begin() + rp32[x], en = adj.begin() + rp32[x + 1];
-                const auto it = std::lower_bound(b, en, u, [](const int2& a, int32_t v) { return a.x < v; });
-                if (it == en || it->x != u) {
-                    sym = false;
-                    break;
+        std::atomic<bool> sym{true};
+        host_parallel(n, [&](int64_t lo, int64_t hi) {
+            for (int64_t u = lo; u < hi && sym.load(std::memory_order_relaxed); ++u)
+                for (int32_t k = rp32[u]; k < rp32[u + 1]; ++k) {
+                    const int32_t x = adj[k].x;
+                    const auto b = adj.begin() + rp32[x], en = adj.begin() + rp32[x + 1];
+                    const auto it = std::lower_bound(b, en, (int32_t)u, [](const int2& a, int32_t v) { return a.x < v; });
+                    if (it == en || it->x != (int32_t)u) {
+                        sym.store(false, std::memory_order_relaxed);
+                        return;
+                    }
+                    revw[(size_t)k] = (uint8_t)it->y;
                 }
-                revw[(size_t)k] = (uint8_t)it->y;
-            }
-        if (sym) {
+        });
+        if (sym.load()) {
             FBC_CK(cudaMalloc(&G->d_ord_revw, revw.size()));
             FBC_CK(cudaMemcpyAsync(G->d_ord_revw, revw.data(), revw.size(), cudaMemcpyHostToDevice, g.st));
         }
