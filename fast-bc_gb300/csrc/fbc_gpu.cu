@@ -14,6 +14,7 @@
 #include <mutex>
 #include <numeric>
 #include <string>
+#include <system_error>
 #include <thread>
 #include <climits>
 #include <clocale>
@@ -335,7 +336,11 @@ void host_parallel(int64_t count, F&& fn) {
     for (int i = 0; i < nthr; ++i) {
         const int64_t lo = (int64_t)i * chunk, hi = std::min<int64_t>(count, lo + chunk);
         if (lo >= hi) break;
-        th.emplace_back([&fn, lo, hi] { fn(lo, hi); });
+        try {
+            th.emplace_back([&fn, lo, hi] { fn(lo, hi); });
+        } catch (const std::system_error&) {  // no thread to be had: this chunk here
+            fn(lo, hi);
+        }
     }
     for (auto& x : th) x.join();
 }
@@ -441,7 +446,11 @@ std::vector<int32_t> bisection_order(int32_t n, const std::vector<int64_t>& rp, 
             }
         };
         std::vector<std::thread> th;
-        for (int i = 0; i < nthr; ++i) th.emplace_back(work);
+        try {
+            for (int i = 0; i < nthr; ++i) th.emplace_back(work);
+        } catch (const std::system_error&) {  // fewer threads than asked: the ones running finish
+        }
+        if (th.empty()) work();
         for (auto& x : th) x.join();
     }
     std::vector<int32_t> nw((size_t)n);
