@@ -3,6 +3,7 @@
 * test_adapters_compile_against_reference (CPU): the drop-in classes of
   include/fastbc_gpu/fastbc_adapters.hpp compile and link against the reference's own interface
   headers (skipped where the reference tree is absent, e.g. on the GPU machine).
+* test_locality_order (CPU): the host locality order against its sequential restatement.
 * test_reference_unit_tests_restated (GPU): tests/cpp/brandes_tests.cpp, the reference's
   Brandes unit tests (ExactBrandesBC.cpp, DijkstraClusterEvaluator.cpp, DijkstraSSBrandesBC.cpp)
   restated against include/fastbc_gpu/engine.hpp, built with g++ and run on the GPU.
@@ -40,6 +41,20 @@ def test_adapters_compile_against_reference(tmp_path):
            os.path.join(ROOT, "tests", "cpp", "adapter_compile.cpp"), "-o", str(out)]
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-2000:]
+
+
+def test_locality_order(tmp_path):
+    """The host locality order (csrc/host_order.hpp, no GPU): the thread-pool bisection equals the
+    sequential recursion on graphs with many components, paths, empty and random directed graphs,
+    and keeps a road grid's edges within short id distances."""
+    gxx = _gxx()
+    exe = tmp_path / "order_test"
+    r = subprocess.run([gxx, "-std=c++17", "-O2", "-pthread", "-I", os.path.join(ROOT, "fast-bc_gb300", "csrc"),
+                        os.path.join(ROOT, "tests", "cpp", "order_test.cpp"), "-o", str(exe)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-2000:]
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0 and "all passed" in r.stdout, r.stdout[-2000:]
 
 
 @pytest.mark.gpu
