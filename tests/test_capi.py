@@ -60,7 +60,11 @@ def test_header_is_plain_c(tmp_path):
 
 OPTIONS = ["delta", "block_threads", "frontier_threads", "group", "chunk_max", "wide_n", "warp_max_n",
            "order_min_n", "iter_mult", "ws_budget_mb", "csr_device_min_m", "wide_threads", "debug_sched",
-           "scratch_keep_mb"]
+           "scratch_keep_mb", "wide_kv", "adj4", "bc_sweep", "pull_count", "source_order"]
+
+# defaults the header documents (a fresh process reads them before anything sets an option)
+DEFAULTS = {"wide_threads": 1024, "wide_kv": 1, "adj4": 1, "bc_sweep": 1, "pull_count": 1, "source_order": 1,
+            "order_min_n": 65536, "scratch_keep_mb": 8192}
 
 
 def test_options_round_trip_and_limits():
@@ -85,7 +89,8 @@ def test_options_round_trip_and_limits():
         return v.value
 
     try:
-        for k, v in [("delta", 37), ("chunk_max", 64), ("group", 2), ("order_min_n", 0), ("iter_mult", 3)]:
+        for k, v in [("delta", 37), ("chunk_max", 64), ("group", 2), ("order_min_n", 0), ("iter_mult", 3),
+                     ("pull_count", 0), ("source_order", 0), ("bc_sweep", 0), ("adj4", 0), ("wide_kv", 2)]:
             assert lib.fbc_set_option(k.encode(), v) == 0 and get(k) == v
         assert lib.fbc_set_option(b"block_threads", 5000) == 0 and get("block_threads") == 1024
         assert lib.fbc_set_option(b"frontier_threads", 1) == 0 and get("frontier_threads") == 32
@@ -98,6 +103,26 @@ def test_options_round_trip_and_limits():
     finally:
         for k, v in saved.items():
             lib.fbc_set_option(k.encode(), v)
+
+
+def test_option_defaults():
+    """A freshly loaded library reports the defaults the header documents."""
+    import json
+    import subprocess
+    import sys
+
+    code = ("import ctypes as C, json, sys\n"
+            "lib = C.CDLL(sys.argv[1])\n"
+            "lib.fbc_get_option.argtypes = [C.c_char_p, C.POINTER(C.c_int64)]\n"
+            "out = {}\n"
+            "for k in sys.argv[2:]:\n"
+            "    v = C.c_int64()\n"
+            "    assert lib.fbc_get_option(k.encode(), C.byref(v)) == 0\n"
+            "    out[k] = v.value\n"
+            "print(json.dumps(out))\n")
+    r = subprocess.run([sys.executable, "-c", code, LIB, *DEFAULTS], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stderr[-2000:]
+    assert json.loads(r.stdout) == DEFAULTS
 
 
 def test_every_entry_point_refuses_cleanly_before_init():
